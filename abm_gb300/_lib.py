@@ -1,0 +1,144 @@
+"""ctypes bindings of ``libabm_vpf.so`` (declared in include/abm_vpf.h).
+
+The library is the product: there is no CPU fallback.  Loading fails loudly when the
+shared library is missing (build it with ``python -m abm_gb300._build``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import _build
+
+c_int32 = ctypes.c_int32
+c_double = ctypes.c_double
+c_void_p = ctypes.c_void_p
+c_float_p = ctypes.POINTER(ctypes.c_float)
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_u32_p = ctypes.POINTER(ctypes.c_uint32)
+c_u64_p = ctypes.POINTER(ctypes.c_ulonglong)
+c_i32_p = ctypes.POINTER(ctypes.c_int32)
+
+ABM_OK = 0
+ABM_WARN_PHI_MISMATCH = 1
+ABM_ERR_INVALID_ARG = -1
+ABM_ERR_RV = -2
+ABM_ERR_CUDA = -3
+ABM_ERR_TIMEOUT = -4
+ABM_ERR_NONFINITE = -5
+ABM_ERR_UNSUPPORTED = -6
+ABM_ERR_NO_DEVICE = -7
+ABM_MAX_RV = 16384
+ABM_DIAG_COUNT = 8
+DIAG_PAIRS_RESOLVED, DIAG_NEAR_BOUNDARY, DIAG_NONFINITE, DIAG_TIMEOUTS = 0, 1, 2, 3
+
+
+class AbmVfParams(ctypes.Structure):
+    _fields_ = [("gam", c_double), ("v0", c_double), ("alp0", c_double), ("alp1", c_double),
+                ("alp2", c_double), ("bet0", c_double), ("bet1", c_double), ("bet2", c_double),
+                ("boundary", c_int32), ("limit_movement", c_int32), ("max_vel", c_double),
+                ("max_th", c_double), ("width", c_double), ("height", c_double),
+                ("window_pad", c_double), ("fov0", c_double), ("fov1", c_double),
+                ("rv", c_int32), ("reserved0", c_int32), ("radius", c_double),
+                ("dt", c_double)]
+
+
+class AbmSwarmState(ctypes.Structure):
+    _fields_ = [("x", c_float_p), ("y", c_float_p), ("theta", c_float_p), ("v", c_float_p)]
+
+
+class AbmAgentOverrides(ctypes.Structure):
+    _fields_ = [("radius", c_float_p), ("alp0", c_float_p), ("bet0", c_float_p),
+                ("v0", c_float_p)]
+
+
+# (name, restype, argtypes) of every exported entry point of include/abm_vpf.h
+SIGNATURES = [
+    ("abm_vpf_abi_version", c_int32, []),
+    ("abm_last_error_string", ctypes.c_char_p, []),
+    ("abm_vf_params_default", c_int32, [ctypes.POINTER(AbmVfParams)]),
+    ("abm_phi_table", c_int32, [c_int32, c_double_p, c_int32]),
+    ("abm_vpf_words", c_int32, [c_int32]),
+    ("abm_vpf_flock_step", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
+      ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_u32_p, c_double_p,
+      c_u64_p, c_void_p]),
+    ("abm_vpf_project_rows", c_int32,
+     [c_double_p, c_int32, c_double_p, c_double, c_double, c_int32, c_double_p, c_double_p,
+      c_int32, c_double, c_double, c_double, c_double_p, c_u64_p, c_void_p]),
+    ("abm_vswrm_integrals", c_int32,
+     [c_int32, c_int32, c_u32_p, c_double_p, c_float_p, c_double_p, c_float_p, c_float_p,
+      c_float_p, c_double_p, c_void_p]),
+    ("abm_vpf_set_step_config", c_int32, [c_int32, c_int32]),
+    ("abm_vpf_get_step_config", c_int32, [c_i32_p, c_i32_p]),
+    ("abm_probe_pipe_peak", c_int32,
+     [c_int32, c_int32, c_int32, c_int32, c_float_p, c_double_p, c_void_p]),
+]
+
+_lock = threading.Lock()
+_lib = None
+
+
+class AbmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"abm_vpf error {code}: {msg}")
+        self.code = code
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed and allowed) the CUDA library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB_PATH
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"abm_gb300 CUDA library not found at {path}; "
+                               "run `python -m abm_gb300._build`")
+        L = ctypes.CDLL(path)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def check(status: int, what: str = "") -> int:
+    """Raise AbmError on a negative status; return warnings (positive) unchanged."""
+    if status < 0:
+        msg = load().abm_last_error_string().decode(errors="replace")
+        raise AbmError(status, f"{what}: {msg}" if what else msg)
+    return status
+
+
+def fptr(t):
+    """float* of a contiguous float32 torch tensor (or None)."""
+    if t is None:
+        return None
+    return ctypes.cast(t.data_ptr(), c_float_p)
+
+
+def dptr(t):
+    if t is None:
+        return None
+    return ctypes.cast(t.data_ptr(), c_double_p)
+
+
+def u32ptr(t):
+    if t is None:
+        return None
+    return ctypes.cast(t.data_ptr(), c_u32_p)
+
+
+def u64ptr(t):
+    if t is None:
+        return None
+    return ctypes.cast(t.data_ptr(), c_u64_p)

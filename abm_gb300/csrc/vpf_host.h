@@ -1,0 +1,32 @@
+// vpf_host.h -- host-side helpers shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "vpf_common.cuh"
+
+namespace abm {
+
+int set_error(int code, const char *fmt, ...);
+int check_cuda(cudaError_t e, const char *what);
+
+// Host copies of one grid's tables (built in FP64 / long double).
+struct GridHostTables {
+    GridDev g;                       // device pointers unset
+    std::vector<float> mid, cot2;
+    std::vector<long long> q, cpt;
+};
+
+int build_grid_host(int rv, double fov0, double fov1, GridHostTables &t);
+
+// Cached device tables for (current device, rv, fov); built synchronously on first use.
+const GridDev *grid_for(int rv, double fov0, double fov1, int *status);
+// Integration-only tables for an explicit Phi grid (abm_vswrm_integrals).
+const GridDev *grid_for_phi(int rv, const double *phi, int *status);
+
+int np_arange_phi(int rv, std::vector<double> *out);
+void np_linspace_pi(int n, std::vector<double> &out);
+int find_nearest(const std::vector<double> &a, double v);
+
+}  // namespace abm

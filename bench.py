@@ -1,0 +1,358 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 visual-flocking hot path (agent-steps/s).
+
+Headline workload: the large single swarm -- N=4096 visual-flocking agents, radius 5,
+5000x5000 walled arena, Rv=3600 over a 2*pi field of view, headings von Mises (kappa=2)
+around a seeded mean, alpha0=beta0=1, alpha1=beta1=0.08, FP32 state, bitmask VPF.  One
+bench step = one simulation timestep of the whole swarm (N agent-steps) through
+abm_vpf_flock_step.  Inputs are seeded synthetic swarms (the reference publishes no dataset).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`value` is kernel-only throughput with the state resident in HBM; `e2e` is the same metric
+through the C-ABI call a per-step host loop makes (pinned host state -> H2D -> step ->
+D2H every step).  The working set (~130 KB) is far below L2, so L2 is flushed (a 256 MiB
+write) between timed steps and only the step itself is inside the CUDA events.
+`--impl reference` times the reference algorithm's CPU restatement (the FP64 C port under
+oracle/, all host threads) on a bounded sample of focal agents of the same workload.
+Multi-GPU runs are independent replicas (the path does not shard across GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "agent-steps/s"
+WORKLOAD = dict(workload="vf_large_swarm", n_agents=4096, radius=5.0, arena=[5000.0, 5000.0],
+                window_pad=30.0, rv=3600, fov="2pi", heading="von Mises kappa=2",
+                alp0=1.0, bet0=1.0, alp1=0.08, bet1=0.08, gam=0.1, v0=1.0, boundary="walls",
+                state="float32", vpf="bitmask", step="one timestep of all agents (Jacobi)",
+                seed=2026)
+# Frozen algorithmic work per agent-step (FP32 ops and MUFU ops), per ordered pair and per
+# agent: F = 36 (N-1) + 4 Rv + 20, M = 3 (N-1).
+F_PAIR, F_PX, F_UPD, M_PAIR = 36, 4, 20, 3
+L2_FLUSH_BYTES = 256 << 20
+# DRAM traffic of one vpf_flock_step launch of this workload, from the ncu capture summarised
+# in profiles/vpf_flock_step_n4096_rv3600.md (dram__bytes_read.sum + dram__bytes_write.sum).
+NCU_TRAFFIC_BYTES = None
+
+
+def make_workload(seed=WORKLOAD["seed"], n=WORKLOAD["n_agents"]):
+    rng = np.random.default_rng(seed)
+    W, H = WORKLOAD["arena"]
+    R, pad = WORKLOAD["radius"], WORKLOAD["window_pad"]
+    x = rng.uniform(pad - R, pad + W - R, n).astype(np.float32)
+    y = rng.uniform(pad - R, pad + H - R, n).astype(np.float32)
+    th = np.mod(rng.vonmises(rng.uniform(0, 2 * np.pi), 2.0, n), 2 * np.pi).astype(np.float32)
+    v = np.zeros(n, np.float32)
+    return {"x": x, "y": y, "theta": th, "v": v}
+
+
+def make_params():
+    from abm_gb300.params import VFParams
+    W, H = WORKLOAD["arena"]
+    return VFParams(gam=0.1, v0=1.0, alp0=1.0, alp1=0.08, bet0=1.0, bet1=0.08,
+                    boundary="walls", width=W, height=H, window_pad=WORKLOAD["window_pad"],
+                    fov=(-math.pi, math.pi), rv=WORKLOAD["rv"], radius=WORKLOAD["radius"])
+
+
+def oracle_params_dict():
+    W, H = WORKLOAD["arena"]
+    return dict(gam=0.1, v0=1.0, alp0=1.0, alp1=0.08, alp2=0.0, bet0=1.0, bet1=0.08, bet2=0.0,
+                boundary=0, limit_movement=0, max_vel=3.0, max_th=0.1, width=W, height=H,
+                window_pad=WORKLOAD["window_pad"], fov0=-math.pi, fov1=math.pi,
+                rv=WORKLOAD["rv"], radius=WORKLOAD["radius"], dt=1.0)
+
+
+# ---------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------- peaks
+def measure_peaks(lib, torch, stream):
+    """Live FP32 (FFMA) and MUFU throughput of this GPU, in ops/s (best of 5)."""
+    import ctypes
+    from abm_gb300 import _lib
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    blocks = props.multi_processor_count * 8
+    sink = torch.zeros(1024, dtype=torch.float32, device="cuda")
+    out = {}
+    for kind, name, iters in ((0, "fp32", 4096), (1, "mufu", 1024)):
+        best = 0.0
+        for _ in range(5):
+            ops = ctypes.c_double()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(lib.abm_probe_pipe_peak(kind, blocks, 256, iters, _lib.fptr(sink),
+                                               ctypes.byref(ops),
+                                               ctypes.c_void_p(stream.cuda_stream)))
+            e1.record(stream)
+            e1.synchronize()
+            best = max(best, ops.value / (e0.elapsed_time(e1) * 1e-3))
+        out[name] = best
+    return out
+
+
+# ---------------------------------------------------------------------- CPU baseline
+def cpu_baseline(state, budget_cpu_s=20.0):
+    """Time the oracle's C port on a bounded sample of focal agents (all host threads)."""
+    import oracle
+    p = oracle_params_dict()
+    threads = oracle.num_threads()
+    t0 = time.perf_counter()
+    oracle.vf_step_range(state, p, 0, threads)
+    t1 = time.perf_counter()
+    per_agent_cpu = (t1 - t0) * threads / threads   # wall of `threads` agents on `threads` cores
+    n_sample = int(max(threads, min(len(state["x"]),
+                                    budget_cpu_s / max(per_agent_cpu, 1e-6))))
+    n_sample = (n_sample // threads) * threads or threads
+    t0 = time.perf_counter()
+    oracle.vf_step_range(state, p, 0, n_sample)
+    wall = time.perf_counter() - t0
+    return {"value": n_sample / wall, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{n_sample} focal agents x 1 step of the N=4096 snapshot "
+                      f"({wall:.1f} s wall), FP64 C restatement with OpenMP",
+            "host_cpus": os.cpu_count()}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import oracle
+    state = make_workload()
+    p = oracle_params_dict()
+    threads = oracle.num_threads()
+    t0 = time.perf_counter()
+    oracle.vf_step_range(state, p, 0, threads)
+    per_round = time.perf_counter() - t0        # one agent per thread
+    budget = 150.0 / max(args.steps + args.warmup, 1)
+    per_step = max(threads, int(budget / max(per_round, 1e-6)) * threads)
+    per_step = min(per_step, len(state["x"]))
+    for _ in range(args.warmup):
+        oracle.vf_step_range(state, p, 0, per_step)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        i0 = (s * per_step) % max(len(state["x"]) - per_step + 1, 1)
+        oracle.vf_step_range(state, p, i0, i0 + per_step)
+    wall = time.perf_counter() - t0
+    value = per_step * args.steps / wall
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(WORKLOAD), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": f"{per_step} focal agents per step of the N=4096 "
+                                       "snapshot; FP64 C restatement of the reference path "
+                                       "(oracle/vpf_oracle.c), OpenMP"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------- GPU arm
+def run_gb300(args, rank, world):
+    import torch
+    import torch.distributed as dist
+    from abm_gb300 import _lib
+    from abm_gb300.swarm import VFSwarm, step_host
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    params = make_params()
+    state = make_workload()
+    n = len(state["x"])
+    sw = VFSwarm(params, state["x"], state["y"], state["theta"], state["v"], device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    peaks = measure_peaks(lib, torch, stream)
+    for _ in range(args.warmup):
+        sw.step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    # ---- kernel-only timed region (state resident in HBM)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier()
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        ev[k][0].record(stream)
+        sw.step()
+        ev[k][1].record(stream)
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    times = np.array([a.elapsed_time(b) for a, b in ev]) * 1e-3
+    kernel_s = float(times.sum())
+
+    # ---- end-to-end through the C-ABI with host buffers (H2D + step + D2H every step)
+    host_in = {k: torch.from_numpy(state[k].copy()).pin_memory() for k in state}
+    host_out = {k: torch.empty(n, dtype=torch.float32).pin_memory() for k in state}
+    dev_in = {k: torch.empty(n, dtype=torch.float32, device=dev) for k in state}
+    dev_out = {k: torch.empty(n, dtype=torch.float32, device=dev) for k in state}
+    cparams = params.to_c()
+    for _ in range(args.warmup):
+        step_host(lib, cparams, n, host_in, host_out, dev_in, dev_out, stream)
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    barrier()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        ev2[k][0].record(stream)
+        step_host(lib, cparams, n, host_in, host_out, dev_in, dev_out, stream)
+        ev2[k][1].record(stream)
+        host_in, host_out = host_out, host_in
+    barrier()
+    e2e_s = float(sum(a.elapsed_time(b) for a, b in ev2)) * 1e-3
+    clk = clocks.stop()
+
+    if world > 1:
+        t = torch.tensor([kernel_s, e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        kernel_s, e2e_s = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+
+    agent_steps = n * args.steps * world
+    value = agent_steps / kernel_s
+    e2e_value = agent_steps / e2e_s
+    t_launch = kernel_s / args.steps
+    rv = WORKLOAD["rv"]
+    F = n * (F_PAIR * (n - 1) + F_PX * rv + F_UPD)
+    M = n * M_PAIR * (n - 1)
+    frac_f = F / t_launch / peaks["fp32"]
+    frac_m = M / t_launch / peaks["mufu"]
+    bound = "fp32" if frac_f >= frac_m else "mufu"
+    achieved = (F if bound == "fp32" else M) / t_launch
+    peak = peaks[bound]
+    roofline = {"bound": bound, "achieved": achieved / 1e12, "peak": peak / 1e12,
+                "unit": "TFLOP/s" if bound == "fp32" else "Tops/s (MUFU)",
+                "frac": achieved / peak,
+                "traffic": NCU_TRAFFIC_BYTES,
+                "algorithmic": {"fp32_ops_per_launch": F, "mufu_ops_per_launch": M,
+                                "fp32_frac": frac_f, "mufu_frac": frac_m,
+                                "hbm_bytes_per_launch": n * 32},
+                "peak_source": "measured live in this run: FFMA-chain and MUFU.RSQ-chain "
+                               "probes (abm_probe_pipe_peak), best of 5",
+                "kernel_ms_mean": t_launch * 1e3,
+                "kernel_ms_p50": float(np.median(times)) * 1e3}
+    diag = sw.diagnostics()
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_launch * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded swarm; the reference publishes no dataset)",
+            "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single",
+                           l2="flushed between timed steps (256 MiB write)"),
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 16 * n,
+                    "d2h_bytes_per_step": 16 * n,
+                    "path": "abm_vpf_flock_step via ctypes, pinned host state, H2D + step + "
+                            "D2H each step"},
+            "gpu_launches": args.steps,
+            "roofline": roofline, "clocks": clk,
+            "wall_s_timed_region": t_wall,
+            "diagnostics": diag}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(state)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)       # rank 0 only; no process group needed
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl")
+    try:
+        run_gb300(args, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

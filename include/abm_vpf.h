@@ -1,0 +1,190 @@
+/*
+ * abm_vpf.h -- C ABI of the GB300 visual-projection-field (VPF) + VSWRM flocking library.
+ *
+ * The library replaces the per-timestep perception and movement path of scioip34/ABM's
+ * visual-flocking agents (reference version 1.2.0):
+ *
+ *   vf_supcalc.projection_field            abm/projects/visual_flocking/vf_agent/vf_supcalc.py:20-138
+ *   vf_supcalc.VSWRM_flocking_state_variables          vf_supcalc.py:161-254 (dPhi_V_of :257-277)
+ *   VFAgent.calc_soc_v_proj / perform_action / update_agent_position
+ *                                           abm/projects/visual_flocking/vf_agent/vf_agent.py:216-327
+ *   Agent.reflect_from_walls / VFAgent.teleport_infinite_arena
+ *                                           abm/agent/agent.py:347-394, vf_agent.py:188-204
+ *   Agent.calc_social_V_proj / projection_field (foraging social channel)
+ *                                           abm/agent/agent.py:396-603
+ *
+ * Conventions
+ *   - Every entry point returns an int status: ABM_OK (0), a positive warning, or a negative
+ *     error; abm_last_error_string() describes the last non-zero status of the calling thread.
+ *   - Array arguments named *_dev are CUDA device pointers; *_host are host pointers.  The
+ *     caller owns all of them.  `stream` is a cudaStream_t passed as void* (NULL = legacy
+ *     default stream).  Calls are stream-ordered and return without synchronising unless
+ *     documented otherwise.
+ *   - Agent state is structure-of-arrays float32: x, y are TOP-LEFT positions (the agent's
+ *     centre is position + radius), theta in [0, 2 pi] with theta = 0 pointing right and
+ *     screen y pointing down, v the scalar speed.  This is the reference's convention.
+ *   - VPF bitmasks: words = ceil(Rv / 32) uint32 per agent; bit (k & 31) of word (k >> 5) is
+ *     raw pixel k, i.e. the pixel order VSWRM integrates (np.flip of the reference's
+ *     returned/stored soc_v_field).  Bits >= Rv are zero.
+ *   - The library allocates device memory only for its cached lookup tables (one set per
+ *     distinct grid: Rv and field of view); the first call for a grid builds them
+ *     synchronously, so make that call before capturing a CUDA graph.
+ */
+#ifndef ABM_VPF_H
+#define ABM_VPF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ABM_VPF_ABI_VERSION 1
+
+/* status codes */
+#define ABM_OK 0
+#define ABM_WARN_PHI_MISMATCH 1      /* len(np.arange(-pi, pi, 2pi/Rv)) != Rv: the reference
+                                        skips the VSWRM update (dv = dpsi = 0) with a printed
+                                        warning, vf_agent.py:268, :283-284 */
+#define ABM_ERR_INVALID_ARG (-1)
+#define ABM_ERR_RV (-2)              /* Rv outside [2, ABM_MAX_RV] */
+#define ABM_ERR_CUDA (-3)
+#define ABM_ERR_TIMEOUT (-4)         /* a bounded device-side wait gave up */
+#define ABM_ERR_NONFINITE (-5)       /* NaN / inf in the agent state */
+#define ABM_ERR_UNSUPPORTED (-6)
+#define ABM_ERR_NO_DEVICE (-7)
+
+#define ABM_MAX_RV 16384
+
+/* boundary conditions (vf_params.BOUNDARY) */
+#define ABM_BOUNDARY_WALLS 0
+#define ABM_BOUNDARY_INFINITE 1
+
+/*
+ * Simulation parameters of one swarm (vf_params.py:12-23 plus the simulation geometry of
+ * abm/simulation/sims.py:60-161).  alp2/bet2 multiply a time derivative that the reference
+ * fixes at zero (vf_supcalc.py:199) and are accepted for completeness only.  dt scales the
+ * heading, speed and position increments; dt = 1 is the reference (it has no dt).
+ */
+typedef struct abm_vf_params {
+    double gam, v0, alp0, alp1, alp2, bet0, bet1, bet2;
+    int32_t boundary;        /* ABM_BOUNDARY_WALLS / ABM_BOUNDARY_INFINITE */
+    int32_t limit_movement;  /* VF_LIMIT_MOVEMENT */
+    double max_vel, max_th;  /* VF_MAX_VEL, VF_MAX_TH */
+    double width, height;    /* arena size (ENV_WIDTH, ENV_HEIGHT) */
+    double window_pad;       /* walls at [pad, pad + width] x [pad, pad + height] */
+    double fov0, fov1;       /* field of view in radians, e.g. (-pi, pi) */
+    int32_t rv;              /* VPF resolution in pixels (after any FOV rescale) */
+    int32_t reserved0;
+    double radius;           /* agent radius when no per-agent radii are given */
+    double dt;               /* 1.0 = reference */
+} abm_vf_params;
+
+/* Device SoA state of n agents (float32, each array n long). */
+typedef struct abm_swarm_state {
+    float *x, *y, *theta, *v;
+} abm_swarm_state;
+
+/* Optional per-agent device arrays (any may be NULL): radius (object_sizes / agent radius),
+ * and the VFAgent.ALP0 / BET0 / V0 heterogeneity overrides (vf_agent.py:24-26). */
+typedef struct abm_agent_overrides {
+    const float *radius, *alp0, *bet0, *v0;
+} abm_agent_overrides;
+
+/* Diagnostics counters (device uint64 array of ABM_DIAG_COUNT, accumulated, never reset by
+ * the library). */
+#define ABM_DIAG_PAIRS_RESOLVED 0    /* pairs whose FP32 decision fell in the guard band and
+                                        were decided again in double-float */
+#define ABM_DIAG_NEAR_BOUNDARY 1     /* of those, pairs whose edge angle lies within 1e-9 rad
+                                        of a pixel / width boundary (reported, not excused) */
+#define ABM_DIAG_NONFINITE 2         /* agents whose state was NaN / inf */
+#define ABM_DIAG_TIMEOUTS 3          /* bounded waits that gave up */
+#define ABM_DIAG_COUNT 8
+
+/* ---------------------------------------------------------------- utilities */
+
+int abm_vpf_abi_version(void);
+const char *abm_last_error_string(void);
+
+/* Reference defaults (vf_params.py:12-23 with the keys unset, sims.py:60-65): GAM 0.1,
+ * V0 1, ALP0 1, ALP1 0.09, BET0 1, BET1 0.09, walls, no limit, MAX_VEL 3, MAX_TH 0.1,
+ * width 600, height 480, pad 30, FOV (-pi, pi), Rv 800, radius 10, dt 1. */
+int abm_vf_params_default(abm_vf_params *p);
+
+/* np.arange(-pi, pi, 2*pi/rv) exactly as numpy builds it (VFAgent.PHI, vf_agent.py:44).
+ * Writes min(length, cap) values to phi_host and returns the length (which is rv + 1 for
+ * the Rv values that trigger the reference's mismatch warning), or a negative error. */
+int abm_phi_table(int32_t rv, double *phi_host, int32_t cap);
+
+/* Number of uint32 words of one VPF bitmask: ceil(rv / 32). */
+int abm_vpf_words(int32_t rv);
+
+/* ---------------------------------------------------------------- hot path */
+
+/*
+ * One snapshot (Jacobi) step of a whole swarm: for every agent, the VPF of all other agents
+ * (projection_field + calc_soc_v_proj, vf_supcalc.py:20-138 / vf_agent.py:216-237), the VSWRM
+ * integrals (vf_supcalc.py:161-277), the heading/speed/position update and the boundary rule
+ * (vf_agent.py:289-327, agent.py:347-394, vf_agent.py:188-204).  Replaces the per-agent loop
+ * of VFAgent.update (vf_agent.py:52-77) driven by VFSimulation.step_sim (vf_sims.py:291-340);
+ * the reference updates agents in place in pygame group order, this call reads `in` and
+ * writes `out` (which must not alias `in`).
+ *
+ * vpf_bits_dev (nullable): n * abm_vpf_words(rv) uint32, the binarised VPF of each agent.
+ * terms_dev (nullable): n * 6 doubles {dvel, dpsi, alpha_blob, alpha_edge, beta_blob,
+ *   beta_edge} = VSWRM_flocking_state_variables(verbose=True) (vf_supcalc.py:241-254).
+ * diag_dev (nullable): ABM_DIAG_COUNT uint64 counters.
+ * Returns ABM_WARN_PHI_MISMATCH (after launching) when the reference would skip VSWRM.
+ */
+int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
+                       const abm_vf_params *p, const abm_agent_overrides *ov,
+                       uint32_t *vpf_bits_dev, double *terms_dev,
+                       unsigned long long *diag_dev, void *stream);
+
+/*
+ * Drop-in twin of vf_supcalc.projection_field (vf_supcalc.py:20-138): the dense per-object
+ * rows of one focal agent, flipped like the reference's return value.
+ * pos_host: focal top-left (x, y) in double; obj_xy_dev: n_obj * 2 doubles (device);
+ * obj_sizes_dev: n_obj doubles or NULL (use radius); vision_range < 0 means None.
+ * rows_dev: n_obj * rv doubles (device), overwritten with 0/1.
+ */
+int abm_vpf_project_rows(const double fov[2], int32_t rv, const double pos_host[2],
+                         double radius, double orientation, int32_t n_obj,
+                         const double *obj_xy_dev, const double *obj_sizes_dev,
+                         int32_t boundary, double width, double height, double vision_range,
+                         double *rows_dev, unsigned long long *diag_dev, void *stream);
+
+/*
+ * Drop-in twin of VSWRM_flocking_state_variables(verbose=True) (vf_supcalc.py:161-254) for a
+ * batch of binary fields given as bitmasks in raw pixel order.  phi_host: the rv values of
+ * the integration grid Phi (any strictly increasing grid; the reference passes
+ * np.arange(-pi, pi, 2pi/rv)).  vel_dev: n_fields floats.  prm: {GAM, V0, ALP0, ALP1, ALP2,
+ * BET0, BET1, BET2}; alp0/bet0/v0_dev optional per-field overrides (NULL = use prm).
+ * out_dev: n_fields * 6 doubles.
+ */
+int abm_vswrm_integrals(int32_t n_fields, int32_t rv, const uint32_t *bits_dev,
+                        const double *phi_host, const float *vel_dev, const double prm[8],
+                        const float *alp0_dev, const float *bet0_dev, const float *v0_dev,
+                        double *out_dev, void *stream);
+
+/* ---------------------------------------------------------------- launch configuration */
+
+/* Warps (focal agents) per block and neighbour-tile length of abm_vpf_flock_step.  0 keeps
+ * the current value.  warps_per_block in {1,2,4,8,16,32}; tile in [32, 8192], multiple of 32. */
+int abm_vpf_set_step_config(int32_t warps_per_block, int32_t tile);
+int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile);
+
+/* ---------------------------------------------------------------- measurement utilities */
+
+/* Pipe-throughput probe (no counterpart in the reference; used for the roofline
+ * denominators): kind 0 launches independent FFMA chains, kind 1 independent MUFU.RSQ chains,
+ * on blocks x threads threads for `iters` rounds.  *ops_out receives the number of FP32 ops
+ * (an FFMA counts 2) or MUFU ops the launch performs; time it with CUDA events on `stream`.
+ * sink_dev: >= threads floats of scratch that keeps the chains live. */
+int abm_probe_pipe_peak(int32_t kind, int32_t blocks, int32_t threads, int32_t iters,
+                        float *sink_dev, double *ops_out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ABM_VPF_H */

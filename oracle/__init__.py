@@ -1,0 +1,250 @@
+"""CPU parity oracle for the visual-flocking hot path (TEST INFRASTRUCTURE ONLY).
+
+The oracle is an FP64 C restatement (``vpf_oracle.c``) of the reference functions
+
+* ``vf_supcalc.projection_field``            abm/projects/visual_flocking/vf_agent/vf_supcalc.py:20-138
+* ``vf_supcalc.calculate_closed_angle``      vf_supcalc.py:142-158
+* ``vf_supcalc.VSWRM_flocking_state_variables`` / ``dPhi_V_of``  vf_supcalc.py:161-277
+* ``VFAgent.calc_soc_v_proj`` / ``perform_action`` / ``update_agent_position``  vf_agent.py:216-327
+* ``Agent.reflect_from_walls`` / ``prove_orientation``  abm/agent/agent.py:347-394, :605-610
+* ``VFAgent.teleport_infinite_arena``       vf_agent.py:188-204
+* ``Agent.calc_social_V_proj`` / ``projection_field`` / ``exlude_V_source_data``  agent.py:396-603
+* ``supcalc.find_nearest`` / ``angle_between``  abm/agent/supcalc.py:8-34
+
+wrapped here with ctypes.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
+leg of ``bench.py`` use it, always as the checker or the timed CPU baseline; the library never
+imports it.  It is pinned against fixtures produced by the reference itself
+(``tests/golden/make_golden.py``) and the reference's own known-answer vectors.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "vpf_oracle.c")
+_OUT_DIR = os.path.join(_HERE, "_build")
+_LIB_PATH = os.path.join(_OUT_DIR, "liborc_vpf.so")
+_lock = threading.Lock()
+_lib = None
+
+# Parameter slots of the oracle's double array (mirror abm_vf_params).
+P_FIELDS = ["gam", "v0", "alp0", "alp1", "alp2", "bet0", "bet1", "bet2", "boundary",
+            "limit_movement", "max_vel", "max_th", "width", "height", "window_pad", "fov0",
+            "fov1", "rv", "radius", "dt"]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library (gcc, OpenMP when available)."""
+    os.makedirs(_OUT_DIR, exist_ok=True)
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(_SRC)):
+        return _LIB_PATH
+    base = ["gcc", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+    tmp = _LIB_PATH + f".tmp{os.getpid()}"
+    try:
+        subprocess.run(base + ["-fopenmp", "-o", tmp, _SRC, "-lm"], check=True,
+                       capture_output=True)
+    except subprocess.CalledProcessError:
+        subprocess.run(base + ["-o", tmp, _SRC, "-lm"], check=True, capture_output=True)
+    os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = build()
+            L = ctypes.CDLL(path)
+            dp = ctypes.POINTER(ctypes.c_double)
+            ip = ctypes.POINTER(ctypes.c_int)
+            u8p = ctypes.POINTER(ctypes.c_uint8)
+            c_int, c_d = ctypes.c_int, ctypes.c_double
+            L.orc_linspace.argtypes = [c_d, c_d, c_int, dp]
+            L.orc_arange.argtypes = [c_d, c_d, c_d, dp, c_int]
+            L.orc_arange.restype = c_int
+            L.orc_find_nearest.argtypes = [dp, c_int, c_d]
+            L.orc_find_nearest.restype = c_int
+            L.orc_angle_between.argtypes = [c_d] * 4
+            L.orc_angle_between.restype = c_d
+            L.orc_closed_angle_vf.argtypes = [c_d] * 4
+            L.orc_closed_angle_vf.restype = c_d
+            L.orc_closed_angle_agent.argtypes = [c_d] * 4
+            L.orc_closed_angle_agent.restype = c_d
+            L.orc_projection_field.argtypes = [c_d, c_d, c_int, c_d, c_d, c_d, c_d, c_int, dp, dp,
+                                               c_int, c_d, c_d, c_d, dp, dp]
+            L.orc_dphi_v.argtypes = [dp, c_int, dp]
+            L.orc_vswrm.argtypes = [c_d, dp, dp, c_int, dp, c_d, c_d, c_d, dp]
+            L.orc_vf_step.argtypes = [c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp, c_int, dp, dp,
+                                      dp, dp, u8p, dp, dp]
+            L.orc_vf_step.restype = c_int
+            L.orc_vf_step_range.argtypes = [c_int, c_int, c_int, dp, dp, dp, dp, dp, dp, dp, dp,
+                                            dp, dp]
+            L.orc_vf_step_range.restype = c_int
+            L.orc_num_threads.restype = c_int
+            L.orc_agent_projection_field.argtypes = [c_int, c_d, c_d, c_d, c_d, c_d, c_d, c_int,
+                                                     c_int, dp, c_int, c_int, dp]
+            L.orc_social_vpf.argtypes = [c_int, c_int, dp, dp, dp, dp, ip, ip, c_d, c_int, c_int,
+                                         c_int, c_d, c_d, dp]
+            _lib = L
+    return _lib
+
+
+def _dp(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def params_array(p) -> np.ndarray:
+    """Pack a parameter mapping / object into the oracle's double array."""
+    get = (lambda k: p[k]) if isinstance(p, dict) else (lambda k: getattr(p, k))
+    return np.array([float(get(k)) for k in P_FIELDS], dtype=np.float64)
+
+
+def linspace(rv: int) -> np.ndarray:
+    out = np.empty(rv, np.float64)
+    lib().orc_linspace(-np.pi, np.pi, rv, _dp(out))
+    return out
+
+
+def arange_phi(rv: int) -> np.ndarray:
+    cap = rv + 8
+    out = np.empty(cap, np.float64)
+    n = lib().orc_arange(-np.pi, np.pi, (2 * np.pi) / rv, _dp(out), cap)
+    return out[:n].copy()
+
+
+def find_nearest(arr, value) -> int:
+    a = _f64(arr)
+    return int(lib().orc_find_nearest(_dp(a), len(a), float(value)))
+
+
+def angle_between(v1, v2) -> float:
+    return float(lib().orc_angle_between(float(v1[0]), float(v1[1]), float(v2[0]), float(v2[1])))
+
+
+def calculate_closed_angle(v1, v2) -> float:
+    return float(lib().orc_closed_angle_vf(float(v1[0]), float(v1[1]), float(v2[0]),
+                                           float(v2[1])))
+
+
+def projection_field(fov, v_field_resolution, position, radius, orientation, object_positions,
+                     object_sizes=None, boundary_cond="walls", arena_width=None,
+                     arena_height=None, vision_range=None, return_margins=False):
+    """Oracle twin of vf_supcalc.projection_field (dense flipped rows)."""
+    objs = _f64(np.asarray(object_positions, dtype=np.float64).reshape(-1, 2))
+    n = objs.shape[0]
+    sizes = None if object_sizes is None else _f64(np.asarray(object_sizes, np.float64))
+    out = np.zeros((n, v_field_resolution), np.float64)
+    marg = np.zeros(n, np.float64)
+    lib().orc_projection_field(float(fov[0]), float(fov[1]), int(v_field_resolution),
+                               float(position[0]), float(position[1]), float(radius),
+                               float(orientation), n, _dp(objs), _dp(sizes),
+                               1 if boundary_cond == "infinite" else 0,
+                               float(arena_width or 0.0), float(arena_height or 0.0),
+                               float("nan") if vision_range is None else float(vision_range),
+                               _dp(out), _dp(marg))
+    return (out, marg) if return_margins else out
+
+
+def dphi_v(V) -> np.ndarray:
+    v = _f64(V)
+    out = np.empty_like(v)
+    lib().orc_dphi_v(_dp(v), len(v), _dp(out))
+    return out
+
+
+def vswrm(vel, Phi, V, params, alp0=None, bet0=None, v0=None) -> np.ndarray:
+    """Oracle twin of VSWRM_flocking_state_variables(verbose=True): 6 values."""
+    phi = _f64(Phi)
+    v = _f64(V)
+    P = params_array(params)
+    out = np.empty(6, np.float64)
+    nan = float("nan")
+    lib().orc_vswrm(float(vel), _dp(phi), _dp(v), len(v), _dp(P),
+                    nan if alp0 is None else float(alp0), nan if bet0 is None else float(bet0),
+                    nan if v0 is None else float(v0), _dp(out))
+    return out
+
+
+def vf_step(state, params, radii=None, alp0=None, bet0=None, v0=None, sequential=False,
+            want_vpf=True, want_terms=True, want_margins=False):
+    """One step of all agents; state = dict of float arrays x, y, theta, v.
+
+    Returns dict with x, y, theta, v (new), vpf (n x Rv uint8 raw order), terms (n x 6),
+    margins (n x n), phi_mismatch (bool)."""
+    x, y, th, v = (_f64(state[k]) for k in ("x", "y", "theta", "v"))
+    n = len(x)
+    P = params_array(params)
+    rv = int(P[17])
+    out = {k: np.empty(n, np.float64) for k in ("x", "y", "theta", "v")}
+    vpf = np.zeros((n, rv), np.uint8) if want_vpf else None
+    terms = np.zeros((n, 6), np.float64) if want_terms else None
+    margins = np.full((n, n), np.inf) if want_margins else None
+    r = _f64(radii)
+    a0, b0, vv0 = _f64(alp0), _f64(bet0), _f64(v0)
+    mism = lib().orc_vf_step(
+        n, _dp(x), _dp(y), _dp(th), _dp(v), _dp(r), _dp(P), _dp(a0), _dp(b0), _dp(vv0),
+        1 if sequential else 0, _dp(out["x"]), _dp(out["y"]), _dp(out["theta"]),
+        _dp(out["v"]),
+        None if vpf is None else vpf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+        _dp(terms), _dp(margins))
+    out.update(vpf=vpf, terms=terms, margins=margins, phi_mismatch=bool(mism))
+    return out
+
+
+def vf_step_range(state, params, i0, i1, radii=None):
+    """Snapshot step of focal agents [i0, i1) only (the bounded CPU-baseline sample)."""
+    x, y, th, v = (_f64(state[k]) for k in ("x", "y", "theta", "v"))
+    n = len(x)
+    P = params_array(params)
+    outs = [np.zeros(n, np.float64) for _ in range(4)]
+    r = _f64(radii)
+    lib().orc_vf_step_range(n, int(i0), int(i1), _dp(x), _dp(y), _dp(th), _dp(v), _dp(r),
+                            _dp(P), *[_dp(o) for o in outs])
+    return outs
+
+
+def num_threads() -> int:
+    return int(lib().orc_num_threads())
+
+
+def agent_projection_field(rv, fov, position, radius, orientation, visual_exclusion,
+                           social_xy, nonsocial_xy=None):
+    """Oracle twin of Agent.projection_field(obstacles, non_expl_agents=...)."""
+    soc = np.asarray(social_xy, np.float64).reshape(-1, 2)
+    has_ns = nonsocial_xy is not None
+    ns = np.asarray(nonsocial_xy if has_ns else np.zeros((0, 2)), np.float64).reshape(-1, 2)
+    xy = _f64(np.concatenate([soc, ns], axis=0))
+    out = np.zeros(rv, np.float64)
+    lib().orc_agent_projection_field(int(rv), float(fov[0]), float(fov[1]), float(position[0]),
+                                     float(position[1]), float(radius), float(orientation),
+                                     1 if visual_exclusion else 0, xy.shape[0], _dp(xy),
+                                     soc.shape[0], 1 if has_ns else 0, _dp(out))
+    return out
+
+
+def social_vpf(i, x, y, radii, theta, exploit, patch, vision_range, visual_exclusion,
+               patchwise, rv, fov):
+    """Oracle twin of Agent.calc_social_V_proj for focal agent i (flipped soc_v_field)."""
+    n = len(x)
+    xs, ys, rs, ts = (_f64(a) for a in (x, y, radii, theta))
+    ex = np.ascontiguousarray(exploit, dtype=np.int32)
+    pa = np.ascontiguousarray(patch, dtype=np.int32)
+    out = np.zeros(rv, np.float64)
+    ipt = ctypes.POINTER(ctypes.c_int)
+    lib().orc_social_vpf(int(i), n, _dp(xs), _dp(ys), _dp(rs), _dp(ts),
+                         ex.ctypes.data_as(ipt), pa.ctypes.data_as(ipt), float(vision_range),
+                         1 if visual_exclusion else 0, 1 if patchwise else 0, int(rv),
+                         float(fov[0]), float(fov[1]), _dp(out))
+    return out

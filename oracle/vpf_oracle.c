@@ -1,0 +1,682 @@
+/*
+ * vpf_oracle.c -- FP64 CPU restatement of the scioip34/ABM visual-flocking hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: the tests, the smoke check and
+ * the CPU-baseline leg of bench.py load it to check (and time) the CUDA library.  Nothing in
+ * the product path links it or falls back to it.
+ *
+ * Every function restates one reference function step by step in IEEE double precision, in
+ * the same operation order numpy uses, so that the oracle reproduces the reference's discrete
+ * decisions (pixel indices, projection widths, wrap rules) and its floating-point results to
+ * within a few ulps.  The pinning evidence is tests/golden/: fixtures produced by running the
+ * reference itself, plus the reference's own known-answer test vectors.
+ *
+ * Compile with -ffp-contract=off (no FMA contraction) so results are the same on x86-64 and
+ * aarch64 hosts.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_PI 3.141592653589793
+
+/* ---------------------------------------------------------------- numpy helpers */
+
+/* np.linspace(start, stop, n): y = arange(n) * step; y += start; y[-1] = stop. */
+void orc_linspace(double start, double stop, int n, double *out)
+{
+    if (n <= 0) return;
+    if (n == 1) { out[0] = start; return; }
+    double delta = stop - start;
+    double step = delta / (double)(n - 1);
+    for (int k = 0; k < n; ++k) {
+        double y = (double)k * step;
+        out[k] = y + start;
+    }
+    out[n - 1] = stop;
+}
+
+/* np.arange(start, stop, step) for doubles: length ceil((stop-start)/step); a[0] = start,
+ * a[1] = start + step, a[i] = start + i * (a[1] - a[0]) (numpy's DOUBLE_fill). Returns the
+ * length; writes at most cap values. */
+int orc_arange(double start, double stop, double step, double *out, int cap)
+{
+    double len_d = ceil((stop - start) / step);
+    int len = len_d > 0 ? (int)len_d : 0;
+    if (len <= 0) return 0;
+    double a0 = start, a1 = start + step;
+    double delta = a1 - a0;
+    for (int i = 0; i < len && i < cap; ++i) {
+        if (i == 0) out[i] = a0;
+        else if (i == 1) out[i] = a1;
+        else out[i] = a0 + (double)i * delta;
+    }
+    return len;
+}
+
+/* supcalc.find_nearest (abm/agent/supcalc.py:8-11): argmin |array - value|, first index on
+ * ties; a NaN value makes every difference NaN and numpy's argmin returns index 0. */
+int orc_find_nearest(const double *arr, int n, double value)
+{
+    if (isnan(value)) return 0;
+    /* two passes (minimum, then its first index) so the O(n) scan vectorises */
+    double bv = fabs(arr[0] - value);
+    for (int k = 1; k < n; ++k) {
+        double d = fabs(arr[k] - value);
+        bv = d < bv ? d : bv;
+    }
+    for (int k = 0; k < n; ++k)
+        if (fabs(arr[k] - value) == bv) return k;
+    return 0;
+}
+
+/* numpy float remainder (npy_divmod): fmod, then shift into the divisor's sign. */
+static double np_remainder(double a, double b)
+{
+    double mod = fmod(a, b);
+    if (mod != 0.0) {
+        if ((b < 0) != (mod < 0)) mod += b;
+    } else {
+        mod = copysign(0.0, b);
+    }
+    return mod;
+}
+
+/* Fill out[a:b] = value with numpy slice semantics (negative indices count from the end,
+ * then clamp to [0, n]). */
+static void np_fill(double *row, int n, long long a, long long b, double value)
+{
+    if (a < 0) { a += n; if (a < 0) a = 0; }
+    if (b < 0) { b += n; if (b < 0) b = 0; }
+    if (a > n) a = n;
+    if (b > n) b = n;
+    for (long long k = a; k < b; ++k) row[k] = value;
+}
+
+/* ---------------------------------------------------------------- geometry */
+
+/* supcalc.angle_between (abm/agent/supcalc.py:14-34). */
+double orc_angle_between(double v1x, double v1y, double v2x, double v2y)
+{
+    double n1 = sqrt(v1x * v1x + v1y * v1y);
+    double u1x = v1x / n1, u1y = v1y / n1;
+    double n2 = sqrt(v2x * v2x + v2y * v2y);
+    double u2x = v2x / n2, u2y = v2y / n2;
+    double dot = u1x * u2x + u1y * u2y;
+    if (dot < -1.0) dot = -1.0;          /* np.clip keeps NaN */
+    if (dot > 1.0) dot = 1.0;
+    double angle = acos(dot);
+    if (u1x * u2y - u1y * u2x < 0) angle = -angle;
+    return angle;
+}
+
+/* vf_supcalc.calculate_closed_angle (vf_supcalc.py:142-158): 0 <= c <= pi is inclusive. */
+double orc_closed_angle_vf(double v1x, double v1y, double v2x, double v2y)
+{
+    double c = np_remainder(orc_angle_between(v1x, v1y, v2x, v2y), 2 * ORC_PI);
+    if (0 <= c && c <= ORC_PI) return -c;
+    return 2 * ORC_PI - c;
+}
+
+/* Agent.projection_field's inline closed angle (agent.py:515-523): 0 < c < pi is strict. */
+double orc_closed_angle_agent(double v1x, double v1y, double v2x, double v2y)
+{
+    double c = np_remainder(orc_angle_between(v1x, v1y, v2x, v2y), 2 * ORC_PI);
+    if (0 < c && c < ORC_PI) return -c;
+    return 2 * ORC_PI - c;
+}
+
+/* Decision margin (radians) of a bearing `ca` and half visual angle `half` on a linspace grid
+ * of Rv pixels: distance of `ca` to the nearest argmin switch (midpoints between grid
+ * points, and the +-pi seam) and of `half` to the nearest floor(proj_size/2) switch
+ * (half = 2*pi*k/Rv).  The tests excuse pixels of pairs whose margin is below 1e-9 rad. */
+static double decision_margin(const double *phis, int Rv, int t, double ca, double half)
+{
+    double m = INFINITY;
+    if (t + 1 < Rv) m = fmin(m, fabs(ca - 0.5 * (phis[t] + phis[t + 1])));
+    if (t >= 1) m = fmin(m, fabs(ca - 0.5 * (phis[t - 1] + phis[t])));
+    m = fmin(m, ORC_PI - fabs(ca));
+    double unit = 2 * ORC_PI / Rv;
+    double k = floor(half / unit);
+    m = fmin(m, fabs(half - k * unit));
+    m = fmin(m, fabs((k + 1) * unit - half));
+    return m;
+}
+
+/* The runs one object contributes to the raw (unflipped) row: up to three [a, b) slices in
+ * numpy slice semantics; returns the number written (0 when the object is skipped or not
+ * visible).  Shared by the dense-row and the union forms below. */
+static int projection_runs(const double *phis, int Rv, int f0, int f1, double acx, double acy,
+                           double v1x, double v1y, double px, double py, double ox, double oy,
+                           double size, int infinite, double W, double H, double vision_range,
+                           long long runs[6], double *margin)
+{
+    if (margin) *margin = INFINITY;
+    if (ox == px && oy == py) return 0;
+    double ocx = ox + size, ocy = oy + size;
+    double v2x = ocx - acx, v2y = ocy - acy;
+    if (infinite) {
+        if (fabs(v2x) > W / 2) {
+            if (acx < ocx) ocx -= W;
+            else if (acx > ocx) ocx += W;
+        }
+        if (fabs(v2y) > H / 2) {
+            if (acy < ocy) ocy -= H;
+            else if (acy > ocy) ocy += H;
+        }
+        v2x = ocx - acx;
+        v2y = ocy - acy;
+    }
+    double ca = orc_closed_angle_vf(v1x, v1y, v2x, v2y);
+    double dx = ocx - acx, dy = ocy - acy;
+    double dist = sqrt(dx * dx + dy * dy);
+    if (!isnan(vision_range) && dist > vision_range) return 0;
+    double vis = 2 * atan(size / (1 * dist));
+    int t = orc_find_nearest(phis, Rv, ca);
+    double ps = (vis / (2 * ORC_PI)) * Rv;
+    long long s = (long long)((double)t - floor(ps / 2));
+    long long e = (long long)((double)t + floor(ps / 2));
+    if (margin) *margin = decision_margin(phis, Rv, t, ca, vis / 2);
+    int nr = 0;
+    if ((f0 < s && s < f1) || (f0 < e && e < f1)) {
+        if (s < 0) { runs[2 * nr] = Rv + s; runs[2 * nr + 1] = Rv; ++nr; s = 0; }
+        if (e >= Rv) { runs[2 * nr] = 0; runs[2 * nr + 1] = e - (Rv - 1); ++nr; e = Rv; }
+        runs[2 * nr] = s; runs[2 * nr + 1] = e; ++nr;
+    }
+    return nr;
+}
+
+/* OR of all objects' rows in raw pixel order (calc_soc_v_proj's sum + binarise,
+ * vf_agent.py:233-236, without materialising the n x Rv rows). */
+void orc_projection_union(double fov0, double fov1, int Rv, double px, double py, double radius,
+                          double orientation, int n, const double *obj_xy,
+                          const double *obj_sizes, int infinite, double W, double H,
+                          double *V, double *margins)
+{
+    double *phis = (double *)malloc(sizeof(double) * (size_t)Rv);
+    orc_linspace(-ORC_PI, ORC_PI, Rv, phis);
+    int f0 = orc_find_nearest(phis, Rv, fov0), f1 = orc_find_nearest(phis, Rv, fov1);
+    double acx = px + radius, acy = py + radius;
+    double aex = px + (1 + cos(orientation)) * radius;
+    double aey = py + (1 - sin(orientation)) * radius;
+    double v1x = aex - acx, v1y = aey - acy;
+    for (int k = 0; k < Rv; ++k) V[k] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        long long runs[6];
+        int nr = projection_runs(phis, Rv, f0, f1, acx, acy, v1x, v1y, px, py, obj_xy[2 * i],
+                                 obj_xy[2 * i + 1], obj_sizes ? obj_sizes[i] : radius, infinite,
+                                 W, H, NAN, runs, margins ? &margins[i] : NULL);
+        for (int r = 0; r < nr; ++r) np_fill(V, Rv, runs[2 * r], runs[2 * r + 1], 1.0);
+    }
+    free(phis);
+}
+
+/*
+ * vf_supcalc.projection_field (vf_supcalc.py:20-138).
+ * obj_xy: n objects as (x, y) top-left positions; obj_sizes may be NULL (use `radius`).
+ * infinite != 0 selects the torus minimal image (boundary_cond == "infinite").
+ * vision_range: NaN means None.
+ * out: n x Rv rows, flipped along the pixel axis like the reference's return value.
+ * margins (nullable): per object, the decision margin in radians (INFINITY when skipped).
+ */
+void orc_projection_field(double fov0, double fov1, int Rv, double px, double py, double radius,
+                          double orientation, int n, const double *obj_xy, const double *obj_sizes,
+                          int infinite, double W, double H, double vision_range, double *out,
+                          double *margins)
+{
+    double *phis = (double *)malloc(sizeof(double) * (size_t)Rv);
+    double *raw = (double *)malloc(sizeof(double) * (size_t)Rv);
+    orc_linspace(-ORC_PI, ORC_PI, Rv, phis);
+    /* fov_px (vf_supcalc.py:105) */
+    int f0 = orc_find_nearest(phis, Rv, fov0), f1 = orc_find_nearest(phis, Rv, fov1);
+    double acx = px + radius, acy = py + radius;
+    double aex = px + (1 + cos(orientation)) * radius;
+    double aey = py + (1 - sin(orientation)) * radius;
+    double v1x = aex - acx, v1y = aey - acy;
+    for (int i = 0; i < n; ++i) {
+        long long runs[6];
+        for (int k = 0; k < Rv; ++k) raw[k] = 0.0;
+        int nr = projection_runs(phis, Rv, f0, f1, acx, acy, v1x, v1y, px, py, obj_xy[2 * i],
+                                 obj_xy[2 * i + 1], obj_sizes ? obj_sizes[i] : radius, infinite,
+                                 W, H, vision_range, runs, margins ? &margins[i] : NULL);
+        for (int r = 0; r < nr; ++r) np_fill(raw, Rv, runs[2 * r], runs[2 * r + 1], 1.0);
+        /* np.flip(v_field, axis=1) (vf_supcalc.py:134) */
+        for (int k = 0; k < Rv; ++k) out[(size_t)i * Rv + k] = raw[Rv - 1 - k];
+    }
+    free(raw);
+    free(phis);
+}
+
+/* ---------------------------------------------------------------- VSWRM */
+
+/* vf_supcalc.dPhi_V_of (vf_supcalc.py:257-277). */
+void orc_dphi_v(const double *V, int n, double *out)
+{
+    /* raw = diff(wrap-pad(V, 1)): raw[0] = V[0]-V[n-1]; raw[k] = V[k]-V[k-1]; raw[n] = raw[0] */
+    double r0 = V[0] - V[n - 1];
+    int backward = (r0 > 0) && (r0 > 0);
+    for (int k = 0; k < n; ++k) {
+        if (backward) out[k] = (k == 0) ? r0 : V[k] - V[k - 1];
+        else out[k] = (k == n - 1) ? r0 : V[k + 1] - V[k];
+    }
+}
+
+static double trapz(const double *y, const double *x, int n)
+{
+    double s = 0.0;
+    for (int k = 0; k + 1 < n; ++k) s += ((x[k + 1] - x[k]) * (y[k + 1] + y[k])) / 2.0;
+    return s;
+}
+
+/*
+ * vf_supcalc.VSWRM_flocking_state_variables (vf_supcalc.py:161-254), verbose form.
+ * prm = {GAM, V0, ALP0, ALP1, ALP2, BET0, BET1, BET2}; alp0/bet0/v0 override when not NaN
+ * (the per-agent ALP0/BET0/V0 arguments).  out = {dvel, dpsi, alpha_blob, alpha_edge,
+ * beta_blob, beta_edge}.
+ */
+void orc_vswrm(double vel, const double *Phi, const double *V, int n, const double *prm,
+               double alp0, double bet0, double v0, double *out)
+{
+    double GAM = prm[0], ALP1 = prm[3], ALP2 = prm[4], BET1 = prm[6], BET2 = prm[7];
+    double ALP0 = isnan(alp0) ? prm[2] : alp0;
+    double BET0 = isnan(bet0) ? prm[5] : bet0;
+    double V0 = isnan(v0) ? prm[1] : v0;
+    double *dphi = (double *)malloc(sizeof(double) * (size_t)n);
+    double *yc = (double *)malloc(sizeof(double) * (size_t)n);
+    double *ys = (double *)malloc(sizeof(double) * (size_t)n);
+    orc_dphi_v(V, n, dphi);
+    double ecos = 0.0, esin = 0.0;
+    for (int k = 0; k < n; ++k) {
+        double gv = -V[k] + ALP2 * 0.0;
+        double gp = -V[k] + BET2 * 0.0;
+        double sp = dphi[k] * dphi[k];
+        yc[k] = cos(Phi[k]) * gv;
+        ys[k] = sin(Phi[k]) * gp;
+        ecos += cos(Phi[k]) * sp;
+        esin += sin(Phi[k]) * sp;
+    }
+    double alpha_blob = ALP0 * trapz(yc, Phi, n);
+    double alpha_edge = ALP0 * ALP1 * ecos;
+    double beta_blob = BET0 * trapz(ys, Phi, n);
+    double beta_edge = BET0 * BET1 * esin;
+    out[0] = GAM * (V0 - vel) + alpha_blob + alpha_edge;
+    out[1] = beta_blob + beta_edge;
+    out[2] = alpha_blob;
+    out[3] = alpha_edge;
+    out[4] = beta_blob;
+    out[5] = beta_edge;
+    free(dphi);
+    free(yc);
+    free(ys);
+}
+
+/* ---------------------------------------------------------------- agent update */
+
+/* Agent.prove_orientation (agent.py:605-610). */
+static double prove_orientation(double th)
+{
+    if (th < 0) th = 2 * ORC_PI + th;
+    if (th > ORC_PI * 2) th = th - 2 * ORC_PI;
+    return th;
+}
+
+static double np_sign_nonzero(double a) { return a > 0 ? 1.0 : (a < 0 ? -1.0 : 1.0); }
+
+/*
+ * Simulation parameters, one double array (mirrors abm_vf_params of include/abm_vpf.h):
+ *  [0] GAM [1] V0 [2] ALP0 [3] ALP1 [4] ALP2 [5] BET0 [6] BET1 [7] BET2
+ *  [8] boundary (0 walls, 1 infinite) [9] limit_movement [10] max_vel [11] max_th
+ *  [12] width [13] height [14] window_pad [15] fov0 [16] fov1 [17] Rv [18] radius [19] dt
+ */
+enum { P_GAM, P_V0, P_ALP0, P_ALP1, P_ALP2, P_BET0, P_BET1, P_BET2, P_BOUNDARY, P_LIMIT,
+       P_MAXVEL, P_MAXTH, P_W, P_H, P_PAD, P_FOV0, P_FOV1, P_RV, P_RADIUS, P_DT, P_COUNT };
+
+/* VFAgent.update_agent_position (vf_agent.py:289-309) with prove_turning/prove_velocity
+ * (:311-327), then reflect_from_walls (agent.py:347-394) or teleport_infinite_arena
+ * (vf_agent.py:188-204).  dt scales the increments (dt = 1 is the reference). */
+static void update_agent(const double *P, double R, double dpsi, double dv, double *x, double *y,
+                         double *th, double *v)
+{
+    double dt = P[P_DT];
+    double theta = dpsi * dt;
+    if (P[P_LIMIT] != 0) {
+        if (fabs(theta) > P[P_MAXTH]) theta = P[P_MAXTH] * np_sign_nonzero(theta);
+    }
+    *th += theta;
+    *th = prove_orientation(*th);
+    *v += dv * dt;
+    if (P[P_LIMIT] != 0) {
+        if (fabs(*v) > P[P_MAXVEL]) *v = P[P_MAXVEL] * np_sign_nonzero(*v);
+    }
+    double nx = *x + (*v * dt) * cos(*th);
+    double ny = *y - (*v * dt) * sin(*th);
+    *x = nx;
+    *y = ny;
+
+    double pad = P[P_PAD];
+    double bx0 = pad, bx1 = pad + P[P_W], by0 = pad, by1 = pad + P[P_H];
+    double cx = *x + R, cy = *y + R;
+    if (P[P_BOUNDARY] == 0) {
+        if (cx < bx0) {
+            *x = bx0 - R;
+            if (ORC_PI / 2 <= *th && *th < ORC_PI) *th -= ORC_PI / 2;
+            else if (ORC_PI <= *th && *th <= 3 * ORC_PI / 2) *th += ORC_PI / 2;
+            *th = prove_orientation(*th);
+        }
+        if (cx > bx1) {
+            *x = bx1 - R - 1;
+            if (3 * ORC_PI / 2 <= *th && *th < 2 * ORC_PI) *th -= ORC_PI / 2;
+            else if (0 <= *th && *th <= ORC_PI / 2) *th += ORC_PI / 2;
+            *th = prove_orientation(*th);
+        }
+        if (cy < by0) {
+            *y = by0 - R;
+            if (ORC_PI / 2 <= *th && *th <= ORC_PI) *th += ORC_PI / 2;
+            else if (0 <= *th && *th < ORC_PI / 2) *th -= ORC_PI / 2;
+            *th = prove_orientation(*th);
+        }
+        if (cy > by1) {
+            *y = by1 - R - 1;
+            if (3 * ORC_PI / 2 <= *th && *th <= 2 * ORC_PI) *th += ORC_PI / 2;
+            else if (ORC_PI <= *th && *th < 3 * ORC_PI / 2) *th -= ORC_PI / 2;
+            *th = prove_orientation(*th);
+        }
+    } else {
+        if (cx < bx0) *x = bx1 - R;
+        else if (cx > bx1) *x = bx0 + R;
+        if (cy < by0) *y = by1 - R;
+        else if (cy > by1) *y = by0 + R;
+    }
+}
+
+/* One agent's perception + VSWRM + update from the positions in (x, y). Writes the raw
+ * (unflipped) OR-ed VPF into vraw (Rv bytes) when given, the six VSWRM terms, and the new
+ * state into the *_new outputs. */
+static void agent_step(int i, int n, const double *x, const double *y, const double *th,
+                       const double *v, const double *radii, const double *P,
+                       const double *alp0_i, const double *bet0_i, const double *v0_i,
+                       double *xn, double *yn, double *thn, double *vn, uint8_t *vraw,
+                       double *terms, double *margins_row, int *phi_mismatch)
+{
+    int Rv = (int)P[P_RV];
+    double R = radii ? radii[i] : P[P_RADIUS];
+    double *objs = (double *)malloc(sizeof(double) * 2 * (size_t)(n > 1 ? n - 1 : 1));
+    double *sizes = (double *)malloc(sizeof(double) * (size_t)(n > 1 ? n - 1 : 1));
+    double *marg = (double *)malloc(sizeof(double) * (size_t)(n > 1 ? n - 1 : 1));
+    double *V = (double *)calloc((size_t)Rv, sizeof(double));
+    int m = 0;
+    for (int j = 0; j < n; ++j) {
+        if (j == i) continue;               /* agents_of_interest excludes self by id */
+        objs[2 * m] = x[j];
+        objs[2 * m + 1] = y[j];
+        sizes[m] = radii ? radii[j] : P[P_RADIUS];
+        ++m;
+    }
+    /* calc_soc_v_proj (vf_agent.py:216-237): sum of the flipped rows, binarised; VSWRM gets
+     * np.flip of that field, i.e. the OR of the rows in raw pixel order. */
+    orc_projection_union(P[P_FOV0], P[P_FOV1], Rv, x[i], y[i], R, th[i], m, objs, sizes,
+                         P[P_BOUNDARY] != 0, P[P_W], P[P_H], V, marg);
+    if (vraw)
+        for (int k = 0; k < Rv; ++k) vraw[k] = V[k] > 0;
+    if (margins_row) {
+        int r = 0;
+        for (int j = 0; j < n; ++j) {
+            if (j == i) { margins_row[j] = INFINITY; continue; }
+            margins_row[j] = marg[r++];
+        }
+    }
+
+    double PHI[8192 + 8];
+    int nphi = orc_arange(-ORC_PI, ORC_PI, (2 * ORC_PI) / Rv, PHI, 8192 + 8);
+    double out[6] = {0, 0, 0, 0, 0, 0};
+    double dv = 0, dpsi = 0;
+    if (nphi == Rv) {
+        orc_vswrm(v[i], PHI, V, Rv, P, alp0_i ? alp0_i[i] : NAN, bet0_i ? bet0_i[i] : NAN,
+                  v0_i ? v0_i[i] : NAN, out);
+        dv = out[0];
+        dpsi = out[1];
+    } else if (phi_mismatch) {
+        *phi_mismatch = 1;   /* vf_agent.py:283-284: dv = dphi = 0 with a printed warning */
+    }
+    if (terms) memcpy(terms, out, sizeof(out));
+    double nx = x[i], ny = y[i], nth = th[i], nv = v[i];
+    update_agent(P, R, dpsi, dv, &nx, &ny, &nth, &nv);
+    *xn = nx;
+    *yn = ny;
+    *thn = nth;
+    *vn = nv;
+    free(objs);
+    free(sizes);
+    free(marg);
+    free(V);
+}
+
+/*
+ * One simulation step of all n agents (VFSimulation.step_sim, vf_sims.py:291-340, with
+ * agents.update at :302).  sequential = 1 reproduces pygame's Group.update order (agent i
+ * sees the already-moved positions of agents < i); sequential = 0 is the snapshot (Jacobi)
+ * form that the GPU kernels implement.  vraw: n x Rv bytes (nullable); terms: n x 6
+ * (nullable); margins: n x n decision margins (nullable).  Returns 1 when len(PHI) != Rv.
+ */
+int orc_vf_step(int n, const double *x, const double *y, const double *th, const double *v,
+                const double *radii, const double *P, const double *alp0_i,
+                const double *bet0_i, const double *v0_i, int sequential, double *x_out,
+                double *y_out, double *th_out, double *v_out, uint8_t *vraw, double *terms,
+                double *margins)
+{
+    int Rv = (int)P[P_RV];
+    int mismatch = 0;
+    if (sequential) {
+        double *cx = (double *)malloc(sizeof(double) * (size_t)n);
+        double *cy = (double *)malloc(sizeof(double) * (size_t)n);
+        double *ct = (double *)malloc(sizeof(double) * (size_t)n);
+        double *cv = (double *)malloc(sizeof(double) * (size_t)n);
+        memcpy(cx, x, sizeof(double) * (size_t)n);
+        memcpy(cy, y, sizeof(double) * (size_t)n);
+        memcpy(ct, th, sizeof(double) * (size_t)n);
+        memcpy(cv, v, sizeof(double) * (size_t)n);
+        for (int i = 0; i < n; ++i) {
+            double a, b, c, d;
+            agent_step(i, n, cx, cy, ct, cv, radii, P, alp0_i, bet0_i, v0_i, &a, &b, &c, &d,
+                       vraw ? vraw + (size_t)i * Rv : NULL, terms ? terms + 6 * (size_t)i : NULL,
+                       margins ? margins + (size_t)i * n : NULL, &mismatch);
+            cx[i] = a; cy[i] = b; ct[i] = c; cv[i] = d;
+        }
+        memcpy(x_out, cx, sizeof(double) * (size_t)n);
+        memcpy(y_out, cy, sizeof(double) * (size_t)n);
+        memcpy(th_out, ct, sizeof(double) * (size_t)n);
+        memcpy(v_out, cv, sizeof(double) * (size_t)n);
+        free(cx); free(cy); free(ct); free(cv);
+    } else {
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : mismatch)
+        for (int i = 0; i < n; ++i) {
+            int mm = 0;
+            agent_step(i, n, x, y, th, v, radii, P, alp0_i, bet0_i, v0_i, &x_out[i], &y_out[i],
+                       &th_out[i], &v_out[i], vraw ? vraw + (size_t)i * Rv : NULL,
+                       terms ? terms + 6 * (size_t)i : NULL,
+                       margins ? margins + (size_t)i * n : NULL, &mm);
+            mismatch |= mm;
+        }
+    }
+    return mismatch;
+}
+
+/* Snapshot step restricted to focal agents [i0, i1) (the bounded CPU-baseline sample). */
+int orc_vf_step_range(int n, int i0, int i1, const double *x, const double *y, const double *th,
+                      const double *v, const double *radii, const double *P, double *x_out,
+                      double *y_out, double *th_out, double *v_out)
+{
+    int mismatch = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : mismatch)
+    for (int i = i0; i < i1; ++i) {
+        int mm = 0;
+        agent_step(i, n, x, y, th, v, radii, P, NULL, NULL, NULL, &x_out[i], &y_out[i],
+                   &th_out[i], &v_out[i], NULL, NULL, NULL, &mm);
+        mismatch |= mm;
+    }
+    return mismatch;
+}
+
+int orc_num_threads(void)
+{
+#ifdef _OPENMP
+    extern int omp_get_max_threads(void);
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ---------------------------------------------------------------- foraging social channel */
+
+/*
+ * Agent.projection_field (agent.py:457-597) with keep_distance_info = False.
+ * obs_xy: n_obs obstacle top-left positions, the first n_social of them social cues and the
+ * rest (present only when has_non_social) non-social occluders.  Every obstacle centre uses
+ * the focal radius R (agent.py:504-505).  visual_exclusion applies the distance-ordered
+ * interval trimming of exlude_V_source_data (agent.py:421-445).  out: Rv values, flipped and
+ * FOV-masked like the reference's return value.
+ */
+void orc_agent_projection_field(int Rv, double fov0, double fov1, double px, double py, double R,
+                                double orientation, int visual_exclusion, int n_obs,
+                                const double *obs_xy, int n_social, int has_non_social,
+                                double *out)
+{
+    double *phis = (double *)malloc(sizeof(double) * (size_t)Rv);
+    double *raw = (double *)calloc((size_t)Rv, sizeof(double));
+    orc_linspace(-ORC_PI, ORC_PI, Rv, phis);
+    int cap = n_obs > 0 ? n_obs : 1;
+    double *dist = (double *)malloc(sizeof(double) * (size_t)cap);
+    double *vis = (double *)malloc(sizeof(double) * (size_t)cap);
+    long long *ps0 = (long long *)malloc(sizeof(long long) * (size_t)cap);
+    long long *pe0 = (long long *)malloc(sizeof(long long) * (size_t)cap);
+    long long *sx = (long long *)malloc(sizeof(long long) * (size_t)cap);
+    long long *ex = (long long *)malloc(sizeof(long long) * (size_t)cap);
+    int *social = (int *)malloc(sizeof(int) * (size_t)cap);
+    int *order = (int *)malloc(sizeof(int) * (size_t)cap);
+    int m = 0;
+
+    double v1sx = px + R, v1sy = py + R;
+    double v1ex = px + (1 + cos(orientation)) * R;
+    double v1ey = py + (1 - sin(orientation)) * R;
+    double v1x = v1ex - v1sx, v1y = v1ey - v1sy;
+    for (int i = 0; i < n_obs; ++i) {
+        double ox = obs_xy[2 * i], oy = obs_xy[2 * i + 1];
+        if (ox == px && oy == py) continue;
+        double v2ex = ox + R, v2ey = oy + R;
+        double v2x = v2ex - v1sx, v2y = v2ey - v1sy;
+        double ca = orc_closed_angle_agent(v1x, v1y, v2x, v2y);
+        double ddx = v2ex - v1sx, ddy = v2ey - v1sy;
+        double d = sqrt(ddx * ddx + ddy * ddy);
+        double va = 2 * atan(R / (1 * d));
+        int t = orc_find_nearest(phis, Rv, ca);
+        if (fov0 < ca && ca < fov1) {
+            double ps = (va / (2 * ORC_PI)) * Rv;
+            dist[m] = d;
+            vis[m] = va;
+            ps0[m] = (long long)((double)t - ps / 2);
+            pe0[m] = (long long)((double)t + ps / 2);
+            sx[m] = ps0[m];
+            ex[m] = pe0[m];
+            social[m] = has_non_social ? (i < n_social) : 1;
+            ++m;
+        }
+    }
+    if (visual_exclusion) {
+        /* rank_V_source_data("distance"): stable ascending sort (insertion order = index) */
+        for (int a = 0; a < m; ++a) order[a] = a;
+        for (int a = 1; a < m; ++a) {
+            int key = order[a], b = a - 1;
+            while (b >= 0 && dist[order[b]] > dist[key]) { order[b + 1] = order[b]; --b; }
+            order[b + 1] = key;
+        }
+        for (int r = 0; r < m; ++r) {
+            int f = order[r];
+            if (r > 0) {
+                for (int q = 0; q < m; ++q) {
+                    int i = order[q];
+                    if (dist[i] < dist[f]) {
+                        if (sx[f] <= ps0[i] && ps0[i] <= ex[f]) ex[f] = ps0[i];
+                        if (sx[f] <= pe0[i] && pe0[i] <= ex[f]) sx[f] = pe0[i];
+                        if (ps0[i] <= sx[f] && pe0[i] >= ex[f]) { sx[f] = 0; ex[f] = 0; }
+                    }
+                }
+            } else {
+                sx[f] = ps0[f];
+                ex[f] = pe0[f];
+            }
+        }
+    }
+    for (int a = 0; a < m; ++a) {
+        if (!social[a]) continue;          /* remove_nonsocial_V_source_data */
+        long long s = sx[a], e = ex[a];
+        if (s < 0) { np_fill(raw, Rv, Rv + s, Rv, 1.0); s = 0; }
+        if (e >= Rv) { np_fill(raw, Rv, 0, e - Rv, 1.0); e = Rv - 1; }
+        np_fill(raw, Rv, s, e, 1.0);
+    }
+    for (int k = 0; k < Rv; ++k) {
+        double val = raw[Rv - 1 - k];
+        if (phis[k] < fov0) val = 0;
+        if (phis[k] > fov1) val = 0;
+        out[k] = val;
+    }
+    free(phis); free(raw); free(dist); free(vis); free(ps0); free(pe0); free(sx); free(ex);
+    free(social); free(order);
+}
+
+/*
+ * Agent.calc_social_V_proj (agent.py:396-419) for focal agent i: candidates within
+ * vision_range (centre distance with each agent's own radius, supcalc.py:73-78), social =
+ * exploiting agents other than i whose patch differs from i's (when patchwise) and is not -1;
+ * every other candidate only occludes.  exploit[j] != 0 means mode "exploit".
+ * out: Rv values (flipped, FOV-masked) = the agent's soc_v_field.
+ */
+void orc_social_vpf(int i, int n, const double *x, const double *y, const double *radii,
+                    const double *th, const int *exploit, const int *patch, double vision_range,
+                    int visual_exclusion, int patchwise, int Rv, double fov0, double fov1,
+                    double *out)
+{
+    int *inr = (int *)malloc(sizeof(int) * (size_t)n);
+    int *expl = (int *)malloc(sizeof(int) * (size_t)n);
+    int *nonx = (int *)malloc(sizeof(int) * (size_t)n * 2);
+    double *xy = (double *)malloc(sizeof(double) * 2 * (size_t)n * 2);
+    int n_in = 0, n_ex = 0, n_nx = 0;
+    double c1x = x[i] + radii[i], c1y = y[i] + radii[i];
+    for (int j = 0; j < n; ++j) {
+        double c2x = x[j] + radii[j], c2y = y[j] + radii[j];
+        double ddx = c2x - c1x, ddy = c2y - c1y;
+        if (sqrt(ddx * ddx + ddy * ddy) <= vision_range) inr[n_in++] = j;
+    }
+    for (int a = 0; a < n_in; ++a) {
+        int j = inr[a];
+        if (j != i && exploit[j]) expl[n_ex++] = j;
+    }
+    for (int a = 0; a < n_in; ++a) {
+        int j = inr[a], is_ex = 0;
+        for (int b = 0; b < n_ex; ++b) if (expl[b] == j) is_ex = 1;
+        if (!is_ex) nonx[n_nx++] = j;
+    }
+    if (patchwise) {
+        int keep = 0;
+        for (int b = 0; b < n_ex; ++b) {
+            if (patch[expl[b]] == patch[i]) nonx[n_nx++] = expl[b];
+        }
+        for (int b = 0; b < n_ex; ++b)
+            if (patch[expl[b]] != patch[i]) expl[keep++] = expl[b];
+        n_ex = keep;
+    }
+    {
+        int keep = 0;
+        for (int b = 0; b < n_ex; ++b) if (patch[expl[b]] != -1) expl[keep++] = expl[b];
+        n_ex = keep;
+    }
+    int n_obs = 0;
+    for (int b = 0; b < n_ex; ++b) { xy[2 * n_obs] = x[expl[b]]; xy[2 * n_obs + 1] = y[expl[b]]; ++n_obs; }
+    if (visual_exclusion) {
+        for (int b = 0; b < n_nx; ++b) { xy[2 * n_obs] = x[nonx[b]]; xy[2 * n_obs + 1] = y[nonx[b]]; ++n_obs; }
+    }
+    orc_agent_projection_field(Rv, fov0, fov1, x[i], y[i], radii[i], th[i], visual_exclusion,
+                               n_obs, xy, n_ex, visual_exclusion, out);
+    free(inr); free(expl); free(nonx); free(xy);
+}

@@ -1,0 +1,230 @@
+"""GPU parity of the fused flock step (abm_vpf_flock_step) against the reference.
+
+Against the golden fixtures (produced by the reference itself) and against the FP64 oracle
+on seeded swarms.  Bars (from the specification of this path):
+* VPF bits: bit-exact, except pixels of pairs whose edge angle lies within 1e-9 rad of a
+  pixel / width boundary (counted via the oracle's decision margins; excused, reported).
+* VSWRM integrals (dvel, dpsi and the four terms): within 1e-5 relative.
+* New state: the FP64 update rounded to float32: within 2 float32 ulps of the reference.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import load_cases, gpu_available
+from _gpu_helpers import seeded_swarm, excused_pixels
+
+pytestmark = pytest.mark.gpu
+
+TERM_RTOL = 1e-5
+
+
+def _swarm_from(state, p, radii=None, alp0=None, bet0=None, v0=None):
+    from abm_gb300.swarm import VFSwarm
+    from abm_gb300.params import VFParams
+    vp = VFParams(gam=p["gam"], v0=p["v0"], alp0=p["alp0"], alp1=p["alp1"], alp2=p["alp2"],
+                  bet0=p["bet0"], bet1=p["bet1"], bet2=p["bet2"],
+                  boundary="infinite" if p["boundary"] else "walls",
+                  limit_movement=bool(p["limit_movement"]), max_vel=p["max_vel"],
+                  max_th=p["max_th"], width=p["width"], height=p["height"],
+                  window_pad=p["window_pad"], fov=(p["fov0"], p["fov1"]), rv=int(p["rv"]),
+                  radius=p["radius"], dt=p["dt"])
+    return VFSwarm(vp, state["x"], state["y"], state["theta"], state["v"], radius=radii,
+                   alp0=alp0, bet0=bet0, v0=v0)
+
+
+def _check_terms(gpu, ref, what):
+    scale = np.maximum(np.abs(ref), 1e-6)
+    err = np.abs(gpu - ref) / scale
+    assert np.all(err <= TERM_RTOL), (what, float(err.max()))
+
+
+def _check_state(gpu, ref, what):
+    for k in ("x", "y", "theta", "v"):
+        r32 = ref[k].astype(np.float32)
+        ulp = np.spacing(np.abs(r32)).astype(np.float64)
+        diff = np.abs(gpu[k].astype(np.float64) - ref[k])
+        assert np.all(diff <= 2 * ulp + 1e-12), (what, k, float((diff / ulp).max()))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+
+
+def test_golden_steps():
+    for c in load_cases("steps"):
+        p = dict(zip(oracle.P_FIELDS, c["params"]))
+        rv = int(p["rv"])
+        opt = lambda a: a if a.size else None
+        hetero = bool(np.any(c["radii"] != c["radii"][0]))
+        st = {k: c[k] for k in ("x", "y", "theta", "v")}
+        sw = _swarm_from(st, p, c["radii"] if hetero else None, opt(c["alp0"]), opt(c["bet0"]),
+                         opt(c["v0"]))
+        status = sw.step(want_vpf=True, want_terms=True)
+        name = str(c["name"])
+        assert status == (1 if name == "mismatch_rv61" else 0), name
+        ref_vpf = np.unpackbits(c["vpf"], axis=1)[:, :rv]
+        gpu_vpf = sw.vpf_numpy()
+        orc = oracle.vf_step(st, p, radii=c["radii"], alp0=opt(c["alp0"]), bet0=opt(c["bet0"]),
+                             v0=opt(c["v0"]), want_margins=True)
+        for i in range(len(st["x"])):
+            bad = np.where(gpu_vpf[i] != ref_vpf[i])[0]
+            if len(bad):
+                ex = excused_pixels(orc["margins"][i], st, i, p, c["radii"] if hetero else None)
+                assert np.all(ex[bad]), (name, i, bad[:10])
+        terms = sw.terms.cpu().numpy()
+        _check_terms(terms, c["terms"], name)
+        new = sw.state_numpy()
+        _check_state(new, {k: c[k + "_new"] for k in ("x", "y", "theta", "v")}, name)
+
+
+@pytest.mark.parametrize("seed,n,rv,R,W,boundary,kappa", [
+    (1, 2, 8, 10.0, 500.0, 0, None),
+    (2, 3, 64, 10.0, 500.0, 0, None),
+    (3, 10, 1200, 10.0, 500.0, 0, None),
+    (4, 100, 1200, 10.0, 1000.0, 0, None),
+    (5, 100, 1200, 10.0, 300.0, 1, None),
+    (6, 300, 3600, 5.0, 5000.0, 0, 2.0),
+    (7, 257, 3600, 5.0, 800.0, 1, 2.0),
+    (8, 64, 333, 7.0, 200.0, 0, None),
+])
+def test_seeded_parity_vs_oracle(seed, n, rv, R, W, boundary, kappa):
+    p = dict(gam=0.1, v0=1.0, alp0=1.0, alp1=0.08, alp2=0.0, bet0=1.0, bet1=0.08, bet2=0.0,
+             boundary=boundary, limit_movement=0, max_vel=3.0, max_th=0.1, width=W, height=W,
+             window_pad=30.0, fov0=-np.pi, fov1=np.pi, rv=rv, radius=R, dt=1.0)
+    st = seeded_swarm(seed, n, W, W, R=R, kappa=kappa)
+    sw = _swarm_from(st, p)
+    sw.step(want_vpf=True, want_terms=True)
+    orc = oracle.vf_step(st, p, want_margins=True)
+    gpu_vpf = sw.vpf_numpy()
+    n_excused = 0
+    for i in range(n):
+        bad = np.where(gpu_vpf[i] != orc["vpf"][i])[0]
+        if len(bad):
+            ex = excused_pixels(orc["margins"][i], st, i, p)
+            assert np.all(ex[bad]), (i, bad[:10])
+            n_excused += len(bad)
+    _check_terms(sw.terms.cpu().numpy(), orc["terms"], (seed, n, rv))
+    _check_state(sw.state_numpy(), orc, (seed, n, rv))
+    d = sw.diagnostics()
+    assert d["timeouts"] == 0 and d["nonfinite"] == 0
+
+
+def test_full_size_spot_check_cfg2():
+    """N=4096, Rv=3600, R=5 in 5000x5000 (the large-swarm workload): 12 focal agents are
+    recomputed by the oracle from the same snapshot."""
+    n, rv, R, W = 4096, 3600, 5.0, 5000.0
+    p = dict(gam=0.1, v0=1.0, alp0=1.0, alp1=0.08, alp2=0.0, bet0=1.0, bet1=0.08, bet2=0.0,
+             boundary=0, limit_movement=0, max_vel=3.0, max_th=0.1, width=W, height=W,
+             window_pad=30.0, fov0=-np.pi, fov1=np.pi, rv=rv, radius=R, dt=1.0)
+    st = seeded_swarm(42, n, W, W, R=R, kappa=2.0)
+    sw = _swarm_from(st, p)
+    sw.step(want_vpf=True, want_terms=True)
+    gpu_vpf = sw.vpf_numpy()
+    terms = sw.terms.cpu().numpy()
+    new = sw.state_numpy()
+    rng = np.random.default_rng(0)
+    for i in rng.choice(n, 12, replace=False):
+        objs = np.stack([np.delete(st["x"], i), np.delete(st["y"], i)], axis=1)
+        rows, marg = oracle.projection_field((-np.pi, np.pi), rv, [st["x"][i], st["y"][i]], R,
+                                             st["theta"][i], objs, return_margins=True)
+        V = (rows.sum(axis=0) > 0)[::-1].astype(np.uint8)
+        bad = np.where(gpu_vpf[i] != V)[0]
+        assert len(bad) == 0 or np.min(marg) < 1e-9, (i, bad[:10])
+        phi = oracle.arange_phi(rv)
+        ref = oracle.vswrm(st["v"][i], phi, V.astype(np.float64), p)
+        _check_terms(terms[i], ref, i)
+
+
+def test_permutation_invariance_full_size():
+    """The VPF is a union of intervals: reordering the agents must permute the outputs
+    exactly (N=4096, Rv=3600)."""
+    from abm_gb300.params import VFParams
+    from abm_gb300.swarm import VFSwarm
+    n, W = 4096, 5000.0
+    st = seeded_swarm(11, n, W, W, R=5.0, kappa=2.0)
+    vp = VFParams(alp1=0.08, bet1=0.08, width=W, height=W, rv=3600, radius=5.0)
+    a = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+    a.step(want_vpf=True, want_terms=True)
+    perm = np.random.default_rng(3).permutation(n)
+    b = VFSwarm(vp, st["x"][perm], st["y"][perm], st["theta"][perm], st["v"][perm])
+    b.step(want_vpf=True, want_terms=True)
+    assert np.array_equal(a.vpf_numpy()[perm], b.vpf_numpy())
+    assert np.array_equal(a.terms.cpu().numpy()[perm], b.terms.cpu().numpy())
+    sa, sb = a.state_numpy(), b.state_numpy()
+    for k in sa:
+        assert np.array_equal(sa[k][perm], sb[k])
+
+
+def test_launch_configs_agree():
+    """Every (warps per block, tile) configuration gives bit-identical results."""
+    from abm_gb300 import _lib
+    from abm_gb300.params import VFParams
+    from abm_gb300.swarm import VFSwarm
+    lib = _lib.load()
+    st = seeded_swarm(5, 1000, 2000.0, 2000.0, R=5.0)
+    vp = VFParams(width=2000.0, height=2000.0, rv=1200, radius=5.0)
+    outs = []
+    try:
+        for warps, tile in ((8, 2048), (4, 256), (16, 1024), (32, 64), (1, 4096)):
+            _lib.check(lib.abm_vpf_set_step_config(warps, tile))
+            s = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+            s.step(want_vpf=True, want_terms=True)
+            outs.append((s.vpf_numpy(), s.terms.cpu().numpy(), s.state_numpy()))
+    finally:
+        lib.abm_vpf_set_step_config(8, 2048)
+    for o in outs[1:]:
+        assert np.array_equal(o[0], outs[0][0])
+        assert np.array_equal(o[1], outs[0][1])
+        for k in o[2]:
+            assert np.array_equal(o[2][k], outs[0][2][k])
+
+
+def test_unaligned_state_uses_plain_loads():
+    """State arrays that are not 16-byte aligned take the non-TMA staging path; results are
+    identical to the aligned path."""
+    import torch
+    from abm_gb300.params import VFParams
+    from abm_gb300.swarm import VFSwarm
+    st = seeded_swarm(9, 777, 1500.0, 1500.0)
+    vp = VFParams(width=1500.0, height=1500.0, rv=1200)
+    a = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+    a.step(want_vpf=True)
+    b = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+    for k in ("x", "y"):
+        big = torch.zeros(b.n + 1, dtype=torch.float32, device="cuda")
+        big[1:] = b._cur[k]
+        b._cur[k] = big[1:]          # 4-byte offset: not 16-byte aligned
+    b.step(want_vpf=True)
+    assert np.array_equal(a.vpf_numpy(), b.vpf_numpy())
+
+
+def test_polarisation_ensemble_cfg0():
+    """Long runs diverge per trajectory (float32 state); compare the ensemble mean
+    polarisation (data_loader.py:1818-1824) of 48 seeds x 300 steps of the N=10 walls
+    workload between the GPU and the oracle's snapshot dynamics."""
+    from abm_gb300.params import VFParams
+    from abm_gb300.swarm import VFSwarm
+    n, steps, seeds = 10, 300, 48
+    p = dict(gam=0.1, v0=1.0, alp0=1.0, alp1=0.08, alp2=0.0, bet0=1.0, bet1=0.08, bet2=0.0,
+             boundary=0, limit_movement=0, max_vel=3.0, max_th=0.1, width=500.0,
+             height=500.0, window_pad=30.0, fov0=-np.pi, fov1=np.pi, rv=1200, radius=10.0,
+             dt=1.0)
+    vp = VFParams(alp1=0.08, bet1=0.08, width=500.0, height=500.0, rv=1200)
+    pol_g, pol_o = [], []
+    for seed in range(seeds):
+        st = seeded_swarm(100 + seed, n, 500.0, 500.0, vmax=0.0)
+        sw = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+        o = dict(st)
+        for t in range(steps):
+            sw.step()
+            o = oracle.vf_step(o, p, want_vpf=False, want_terms=False)
+        g = sw.state_numpy()
+        pol = lambda th: np.hypot(np.cos(th).sum(), np.sin(th).sum()) / n
+        pol_g.append(pol(g["theta"].astype(np.float64)))
+        pol_o.append(pol(o["theta"]))
+    pol_g, pol_o = np.array(pol_g), np.array(pol_o)
+    se = np.sqrt(pol_g.var() / seeds + pol_o.var() / seeds)
+    assert abs(pol_g.mean() - pol_o.mean()) < 4 * se + 1e-3, (pol_g.mean(), pol_o.mean(), se)
