@@ -196,9 +196,6 @@ __device__ __forceinline__ void exact_offset(const FocalDev &f, float xj, float 
     }
 }
 
-// Double-float re-decision of the pixel index t and/or the half width h of one pair.
-// u: FP32 pixel coordinate of the bearing; ps2: FP32 proj_size/2.  Counts the pair in
-// diag[0], and in diag[1] when a decision lies within 1e-9 rad of its boundary.
 struct ResolveGrid {  // the parts of GridDev the double-float re-decision needs
     const float4 *mid;
     const float2 *cot2;
@@ -210,11 +207,12 @@ __device__ __forceinline__ ResolveGrid resolve_grid(const GridDev &g) {
     return {g.mid, g.cot2, g.rv, g.kmax, g.band_t, g.rvm1};
 }
 
-// Returns the re-decided (t, h).
-static __device__ __noinline__ int2 resolve_pair(dfl cd, dfl sd, dfl ex, dfl ey, float rj,
-                                          ResolveGrid g, bool unc_t, bool unc_h, float u,
-                                          float ps2, int t, int h,
-                                          unsigned long long *diag) {
+// Double-float re-decision of the pixel index t and/or the half width h of one pair.
+// u: FP32 pixel coordinate of the bearing; ps2: FP32 proj_size/2.  Returns (t, h) in x, y and
+// in z whether a re-decided boundary lies within 1e-9 rad of the pair's edge angle.
+static __device__ __noinline__ int3 resolve_pair(dfl cd, dfl sd, dfl ex, dfl ey, float rj,
+                                                 ResolveGrid g, bool unc_t, bool unc_h, float u,
+                                                 float ps2, int t, int h) {
     dfl P = df_add(df_mul(cd, ey), df_mul(sd, ex));  // cross(v1, v2) / R
     dfl Q = df_sub(df_mul(cd, ex), df_mul(sd, ey));  // dot(v1, v2) / R
     dfl d2 = df_add(df_mul(ex, ex), df_mul(ey, ey));
@@ -251,21 +249,14 @@ static __device__ __noinline__ int2 resolve_pair(dfl cd, dfl sd, dfl ex, dfl ey,
             near |= da < 1e-9f;
         }
     }
-    if (diag) {
-        atomicAdd(&diag[0], 1ull);
-        if (near) atomicAdd(&diag[1], 1ull);
-    }
-    return make_int2(t, h);
+    return make_int3(t, h, near ? 1 : 0);
 }
 
-// Full decision for one ordered pair (all 32 lanes call it; `live` masks the lane's pair).
-// Returns the visible projection's (s, e) or vis = false.
+// FP32 centre offset of one ordered pair (exact differences rounded once; the torus image
+// and unequal radii go through the exact double-float offset).
 template <bool TORUS, bool HETERO>
-__device__ __forceinline__ void pair_projection(const FocalDev &f, float xj, float yj, float rj,
-                                                float invrj, bool valid, const GridDev &g,
-                                                dfl W, dfl H, int &s_out, int &e_out,
-                                                bool &vis, unsigned long long *diag) {
-    float dx, dy;
+__device__ __forceinline__ void pair_offset(const FocalDev &f, float xj, float yj, float rj,
+                                            dfl W, dfl H, float &dx, float &dy) {
     if (!TORUS && !HETERO) {
         dx = xj - f.x;
         dy = yj - f.y;
@@ -275,46 +266,95 @@ __device__ __forceinline__ void pair_projection(const FocalDev &f, float xj, flo
         dx = ex.hi + ex.lo;
         dy = ey.hi + ey.lo;
     }
-    bool same = (xj == f.x) && (yj == f.y);   // vf_supcalc.py:57-58 (covers j == i)
-    float d2 = fmaf(dx, dx, dy * dy);
-    bool live = valid && !same && (d2 <= rj * rj * g.cull);
-    float rsq = rsqrtf(d2);
-    float P = fmaf(f.c, dy, f.s * dx);
-    float Q = fmaf(f.c, dx, -(f.s * dy));
-    float ca = closed_angle_f32(P, Q);
-    float u = fmaf(ca, g.inv_delta, g.half_rm1);
-    float kf = floorf(u);
-    float fr = u - kf;
-    int t = (int)kf + (fr > 0.5f ? 1 : 0);
-    t = t < 0 ? 0 : (t > g.rv - 1 ? g.rv - 1 : t);
-    bool unc_t = fabsf(fr - 0.5f) < g.band_t || u < g.band_t || u > g.rvm1 - g.band_t;
-    float al = half_angle_f32(rj, invrj, d2, rsq);
-    float ps2 = al * g.ps2_scale;
-    float hf = floorf(ps2);
-    int h = (int)hf;
-    float frh = ps2 - hf;
-    float bh = g.band_h * fmaxf(ps2, 1.f);
-    bool unc_h = frh < bh || frh > 1.f - bh;
-    if (d2 == 0.f) {  // coincident centres, different top-left: atan(R/0) = pi/2, NaN bearing -> 0
-        t = 0;
-        h = g.rv >> 2;
-        unc_t = unc_h = false;
+}
+
+// FP32 estimate of the pixel index t and half width h of one live pair, with the flags of
+// decisions that fall inside the guard bands.
+struct PairEst {
+    int t, h;
+    float u, ps2;
+    bool unc_t, unc_h;
+};
+
+// Both arctangents of a pair share one packed (FP32x2) Horner chain: lane .x is the bearing
+// ratio, lane .y the half-angle ratio.
+__device__ __forceinline__ float2 atan_poly2(float2 s) {
+    float2 p = make_float2(2.456724644e-03f, 2.456724644e-03f);
+    p = __ffma2_rn(p, s, make_float2(-1.440135855e-02f, -1.440135855e-02f));
+    p = __ffma2_rn(p, s, make_float2(3.978122398e-02f, 3.978122398e-02f));
+    p = __ffma2_rn(p, s, make_float2(-7.234857231e-02f, -7.234857231e-02f));
+    p = __ffma2_rn(p, s, make_float2(1.049894616e-01f, 1.049894616e-01f));
+    p = __ffma2_rn(p, s, make_float2(-1.416122913e-01f, -1.416122913e-01f));
+    p = __ffma2_rn(p, s, make_float2(1.998590678e-01f, 1.998590678e-01f));
+    p = __ffma2_rn(p, s, make_float2(-3.333259821e-01f, -3.333259821e-01f));
+    p = __ffma2_rn(p, s, make_float2(9.999998808e-01f, 9.999998808e-01f));
+    return p;
+}
+
+template <bool HETERO>
+__device__ __forceinline__ PairEst estimate_pair(const FocalDev &f, float dx, float dy, float rj,
+                                                 float invrj, const GridDev &g) {
+    PairEst r;
+    const float d2 = fmaf(dx, dx, dy * dy);
+    const float rsq = rsqrtf(d2);
+    // (P, Q) = (c dy + s dx, c dx - s dy): cross and dot of the heading with the offset
+    const float2 PQ = __ffma2_rn(make_float2(f.c, f.c), make_float2(dy, dx),
+                                 __fmul2_rn(make_float2(f.s, -f.s), make_float2(dx, dy)));
+    const float P = PQ.x, Q = PQ.y;
+    const float ay = fabsf(P), ax = fabsf(Q);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    const float rb = mn * rcp_approx(mx);                  // bearing ratio in [0, 1]
+    const float xr = rj * rsq;                             // R / d
+    const bool big = xr > 1.f;
+    const float rh = big ? (d2 * rsq) * invrj : xr;        // half-angle ratio in [0, 1]
+    const float2 rr = make_float2(rb, rh);
+    const float2 at = __fmul2_rn(rr, atan_poly2(__fmul2_rn(rr, rr)));
+    float a = at.x;
+    a = (ay > ax) ? kHalfPiF - a : a;
+    a = (Q < 0.f) ? kPiF - a : a;
+    const float ca = (P >= 0.f) ? -a : a;
+    const float al = big ? kHalfPiF - at.y : at.y;
+    // (u, ps2): pixel coordinate of the bearing and proj_size / 2
+    const float2 up = __ffma2_rn(make_float2(ca, al), make_float2(g.inv_delta, g.ps2_scale),
+                                 make_float2(g.half_rm1, 0.f));
+    const float u = up.x, ps2 = up.y;
+    const float kf = floorf(u), hf = floorf(ps2);
+    const float2 fr = __fadd2_rn(up, make_float2(-kf - 0.5f, -hf - 0.5f));  // frac - 1/2
+    int t = (int)kf + (fr.x > 0.f ? 1 : 0);
+    r.t = min(max(t, 0), g.rv - 1);
+    r.h = (int)hf;
+    r.unc_t = fabsf(fr.x) < g.band_t || fabsf(u - g.half_rm1) > g.half_rm1 - g.band_t;
+    r.unc_h = fabsf(fr.y) > 0.5f - g.band_h * fmaxf(ps2, 1.f);
+    if (HETERO && d2 == 0.f) {  // coincident centres: atan(R/0) = pi/2, NaN bearing -> pixel 0
+        r.t = 0;
+        r.h = g.rv >> 2;
+        r.unc_t = r.unc_h = false;
     }
-    bool unc = live && (unc_t || unc_h);
-    if (__any_sync(ABM_FULL_MASK, unc)) {
-        if (unc) {
-            dfl ex, ey;
-            exact_offset<TORUS, HETERO>(f, xj, yj, rj, W, H, ex, ey);
-            int2 th = resolve_pair(f.cd, f.sd, ex, ey, rj, resolve_grid(g), unc_t, unc_h, u,
-                                   ps2, t, h, diag);
-            t = th.x;
-            h = th.y;
-        }
+    r.u = u;
+    r.ps2 = ps2;
+    return r;
+}
+
+// Visibility test of vf_supcalc.py:119 (strict, on the pixel indices).
+__device__ __forceinline__ bool projection_visible(const GridDev &g, int s, int e) {
+    return (g.f0 < s && s < g.f1) || (g.f0 < e && e < g.f1);
+}
+
+// OR a visible projection [s, e) into the bitmask; the common case (no wrap, at most 32
+// pixels) is two predicated shared atomics, the rest goes through raster_projection.
+__device__ __forceinline__ void raster_fast(uint32_t *vb, int rv, int s, int e) {
+    const unsigned len = (unsigned)(e - s);
+    if (s >= 0 && e < rv && len <= 32u) {
+        // run mask of `len` ones shifted to bit s & 31, split over words w0, w0 + 1
+        const uint32_t m = len >= 32u ? ABM_FULL_MASK : ((1u << len) - 1u);
+        const int w0 = s >> 5, sh = s & 31;
+        const uint32_t lo = m << sh;
+        const uint32_t hi = __funnelshift_l(m, 0u, sh);
+        if (lo) atomicOr(&vb[w0], lo);
+        if (hi) atomicOr(&vb[w0 + 1], hi);
+    } else {
+        raster_projection(vb, rv, s, e);
     }
-    int s = t - h, e = t + h;
-    vis = live && ((g.f0 < s && s < g.f1) || (g.f0 < e && e < g.f1));
-    s_out = s;
-    e_out = e;
 }
 
 // ------------------------------------------------------------------ VSWRM integrals
@@ -434,6 +474,34 @@ __device__ __forceinline__ void update_agent(const UpdateParams &p, double R, do
         if (cy < p.by0) y = p.by1 - R;
         else if (cy > p.by1) y = p.by0 + R;
     }
+}
+
+// ------------------------------------------------------------------ double-float sincos
+// cos/sin of a float32 angle to ~1e-14 using FP32 arithmetic only (GB300's FP64 pipe is
+// ~1/64 of its FP32 rate, and a lane-masked FP64 instruction costs a full warp's time):
+// theta = k h + r with h = 2 pi / 1024 (Cody-Waite in double-float), a table of cos/sin(k h)
+// (kSinCosTab entries of df pairs, built on the host in FP64), and Taylor series of cos/sin(r)
+// for |r| <= pi / 1024 (truncation errors r^7/5040 and r^6/720 below 2e-18).
+constexpr int kSinCosTab = 1024;
+
+__device__ __forceinline__ void df_sincos(float theta, const float4 *tab, dfl &c, dfl &s) {
+    const float inv_h = 1.629746552e+02f;             // 1024 / (2 pi)
+    const dfl H = {6.135923322e-03f, -1.707476105e-10f};      // 2 pi / 1024 in double-float
+    const float kf = rintf(theta * inv_h);
+    int k = (int)kf;
+    dfl r = df_sub(dfl{theta, 0.f}, df_add(two_prod(kf, H.hi), two_prod(kf, H.lo)));
+    k &= (kSinCosTab - 1);
+    const dfl r2 = df_mul(r, r);
+    // sin r = r (1 - r2 (1/6 - r2/120)),  cos r = 1 - r2 (1/2 - r2/24)
+    const dfl sixth = {1.666666716e-01f, -4.967053879e-09f};
+    const dfl s_in = df_sub(sixth, df_mul(r2, dfl{8.333333768e-03f, -4.346172033e-10f}));
+    const dfl sr = df_mul(r, df_sub(dfl{1.f, 0.f}, df_mul(r2, s_in)));
+    const dfl c_in = df_sub(dfl{0.5f, 0.f}, df_mul(r2, dfl{4.166666791e-02f, -1.241763470e-09f}));
+    const dfl cr = df_sub(dfl{1.f, 0.f}, df_mul(r2, c_in));
+    const float4 t = tab[k];
+    const dfl ck = {t.x, t.y}, sk = {t.z, t.w};
+    c = df_sub(df_mul(ck, cr), df_mul(sk, sr));
+    s = df_add(df_mul(sk, cr), df_mul(ck, sr));
 }
 
 // ------------------------------------------------------------------ TMA bulk staging

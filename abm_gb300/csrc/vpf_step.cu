@@ -1,16 +1,21 @@
-// vpf_step.cu -- the fused per-timestep kernel (VPF rasterisation + VSWRM + update) and the
-// drop-in twins of projection_field / VSWRM_flocking_state_variables.
+// vpf_step.cu -- the per-timestep hot path (VPF rasterisation + VSWRM integrals + agent update)
+// and the drop-in twins of projection_field / VSWRM_flocking_state_variables.
 //
-// Work decomposition: one warp per focal agent.  A block of `warps` focal agents streams the
-// neighbour positions through shared memory in tiles (n-body style), staged by the TMA bulk
-// engine (cp.async.bulk + mbarrier, double-buffered) when the state arrays are 16-byte
-// aligned.  Each lane evaluates one neighbour per iteration, and OR-s the visible pixel run
-// into the warp's VPF bitmask (ceil(Rv/32) words in shared memory).  The warp then walks the
-// bitmask's transitions to form the VSWRM integrals against fixed-point tables and lane 0
-// applies the FP64 state update.
+// One step is two launches:
+//  * a pair kernel: one warp per focal agent evaluates every neighbour (FP32 with a guard band
+//    and a double-float re-decision inside it), OR-s the visible pixel runs into the agent's
+//    VPF bitmask in shared memory and reduces the bitmask's transitions to the four VSWRM sums
+//    (fixed point).  Two forms: `l1` (single-warp blocks, neighbours read through the
+//    read-only L1 path; balanced to ~27 agents per SM, no block barriers) and `tiled`
+//    (several focal warps per block share neighbour tiles staged in shared memory by the TMA
+//    bulk engine, double-buffered with mbarriers; for swarms whose positions do not fit L1);
+//  * an update kernel: one thread per agent applies the FP64 VSWRM combination and the
+//    reference's heading / speed / position update and boundary rule, with all 32 lanes of
+//    every warp busy (a lane-masked FP64 instruction costs a whole warp's FP64 time on GB300).
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 
 #include "../../include/abm_vpf.h"
@@ -30,54 +35,341 @@ struct StepArgs {
     dfl W, H;
     UpdateParams up;
     GridDev g;
+    long long *sums;       // n x 4 workspace: bc, bs, ec, es of every agent
 };
 
-static int g_warps = 8;
-static int g_tile = 2048;
+static int g_warps = 8;    // tiled form: focal warps per block
+static int g_tile = 8192;  // tiled form: neighbour tile length
+static int g_mode = 0;     // 0 auto, 1 l1, 2 tiled
+static int g_wpa = 1;      // l1 form: warps per focal agent
 static std::mutex g_cfg_mu;
 
-static size_t step_smem_bytes(int warps, int tile, int words, bool hetero) {
+// cos/sin(k 2pi/1024) as double-float pairs, read with warp-uniform indices (constant cache).
+__constant__ float4 c_sincos[kSinCosTab];
+
+static int ensure_sincos_table() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 64 && done[dev]) return ABM_OK;
+    float4 tab[kSinCosTab];
+    for (int k = 0; k < kSinCosTab; ++k) {
+        const long double a = (long double)k * 2.0L * 3.14159265358979323846264338327950288L /
+                              (long double)kSinCosTab;
+        const long double c = cosl(a), sn = sinl(a);
+        const float ch = (float)c, sh = (float)sn;
+        tab[k] = make_float4(ch, (float)(c - (long double)ch), sh, (float)(sn - (long double)sh));
+    }
+    int st = check_cuda(cudaMemcpyToSymbol(c_sincos, tab, sizeof(tab)), "sincos table upload");
+    if (!st && dev < 64) done[dev] = true;
+    return st;
+}
+
+// Per-(device, stream) workspace for the per-agent sums (grown on demand, never shrunk).
+static void *workspace(cudaStream_t stream, size_t bytes, int *status) {
+    static std::mutex mu;
+    static std::map<std::pair<int, void *>, std::pair<void *, size_t>> ws;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto &e = ws[{dev, (void *)stream}];
+    if (e.second < bytes) {
+        if (e.first) {
+            cudaStreamSynchronize(stream);
+            cudaFree(e.first);
+        }
+        e = {nullptr, 0};
+        void *p = nullptr;
+        *status = check_cuda(cudaMalloc(&p, bytes), "cudaMalloc(step workspace)");
+        if (*status) return nullptr;
+        e = {p, bytes};
+    }
+    *status = ABM_OK;
+    return e.first;
+}
+
+// Per-warp work queues of the step kernel: candidate neighbours that survived the cull (their
+// positions, so the queue outlives the tile) and pairs whose FP32 decision needs the
+// double-float re-decision.
+constexpr int kQueue = 64;
+constexpr int kQueue2 = 64;
+
+template <bool HETERO>
+struct QEntry;
+template <>
+struct QEntry<false> {
+    float2 v;
+    __device__ __forceinline__ float x() const { return v.x; }
+    __device__ __forceinline__ float y() const { return v.y; }
+    __device__ __forceinline__ float r(float r0) const { return r0; }
+    __device__ __forceinline__ static QEntry make(float x, float y, float) {
+        return QEntry{make_float2(x, y)};
+    }
+};
+template <>
+struct QEntry<true> {
+    float4 v;
+    __device__ __forceinline__ float x() const { return v.x; }
+    __device__ __forceinline__ float y() const { return v.y; }
+    __device__ __forceinline__ float r(float) const { return v.z; }
+    __device__ __forceinline__ static QEntry make(float x, float y, float r) {
+        return QEntry{make_float4(x, y, r, 0.f)};
+    }
+};
+
+// Heavy decision + rasterisation of up to 32 queued candidates (lane < cnt holds one).
+template <bool TORUS, bool HETERO>
+__device__ __forceinline__ void process_candidates(const FocalDev &f, const QEntry<HETERO> *q,
+                                                   int cnt, QEntry<HETERO> *q2, int &q2n,
+                                                   uint32_t *vb, const StepArgs &a,
+                                                   unsigned *cnt_resolved, unsigned *cnt_near) {
+    const int lane = threadIdx.x & 31;
+    const bool have = lane < cnt;
+    QEntry<HETERO> e = have ? q[lane] : QEntry<HETERO>::make(f.x, f.y, f.r);
+    const float xj = e.x(), yj = e.y(), rj = e.r(a.radius0);
+    float dx, dy;
+    pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
+    const PairEst est = estimate_pair<HETERO>(f, dx, dy, rj, HETERO ? rcp_approx(rj) : f.invr,
+                                              a.g);
+    const bool unc = have && (est.unc_t || est.unc_h);
+    const unsigned um = __ballot_sync(ABM_FULL_MASK, unc);
+    if (um) {  // defer the uncertain ones to the double-float queue
+        if (unc) q2[q2n + __popc(um & ((1u << lane) - 1u))] = e;
+        q2n += __popc(um);
+    }
+    const int s = est.t - est.h, en = est.t + est.h;
+    if (have && !unc && projection_visible(a.g, s, en)) raster_fast(vb, a.g.rv, s, en);
+    __syncwarp();
+    if (q2n >= 32) {   // drain 32 deferred pairs (warp-uniform)
+        q2n -= 32;
+        const QEntry<HETERO> d = q2[q2n + lane];
+        const float dxj = d.x(), dyj = d.y(), drj = d.r(a.radius0);
+        float ddx, ddy;
+        pair_offset<TORUS, HETERO>(f, dxj, dyj, drj, a.W, a.H, ddx, ddy);
+        const PairEst de = estimate_pair<HETERO>(f, ddx, ddy, drj,
+                                                 HETERO ? rcp_approx(drj) : f.invr, a.g);
+        dfl ex, ey;
+        exact_offset<TORUS, HETERO>(f, dxj, dyj, drj, a.W, a.H, ex, ey);
+        const int3 th = resolve_pair(f.cd, f.sd, ex, ey, drj, resolve_grid(a.g), de.unc_t,
+                                     de.unc_h, de.u, de.ps2, de.t, de.h);
+        const int ds = th.x - th.y, dn = th.x + th.y;
+        if (projection_visible(a.g, ds, dn)) raster_fast(vb, a.g.rv, ds, dn);
+        const unsigned nm = __ballot_sync(ABM_FULL_MASK, th.z != 0);
+        if (lane == 0) {
+            atomicAdd(cnt_resolved, 32u);
+            if (nm) atomicAdd(cnt_near, (unsigned)__popc(nm));
+        }
+        __syncwarp();
+    }
+}
+
+// Double-float resolution of the last (< 32) deferred pairs.
+template <bool TORUS, bool HETERO>
+__device__ __forceinline__ void drain_deferred(const FocalDev &f, const QEntry<HETERO> *q2,
+                                               int q2n, uint32_t *vb, const StepArgs &a,
+                                               unsigned *cnt_resolved, unsigned *cnt_near) {
+    const int lane = threadIdx.x & 31;
+    if (q2n == 0) return;
+    bool near = false;
+    if (lane < q2n) {
+        const QEntry<HETERO> d = q2[lane];
+        const float xj = d.x(), yj = d.y(), rj = d.r(a.radius0);
+        float dx, dy;
+        pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
+        const PairEst de = estimate_pair<HETERO>(f, dx, dy, rj,
+                                                 HETERO ? rcp_approx(rj) : f.invr, a.g);
+        dfl ex, ey;
+        exact_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, ex, ey);
+        const int3 th = resolve_pair(f.cd, f.sd, ex, ey, rj, resolve_grid(a.g), de.unc_t,
+                                     de.unc_h, de.u, de.ps2, de.t, de.h);
+        const int ds = th.x - th.y, dn = th.x + th.y;
+        if (projection_visible(a.g, ds, dn)) raster_fast(vb, a.g.rv, ds, dn);
+        near = th.z != 0;
+    }
+    const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
+    if (lane == 0) {
+        atomicAdd(cnt_resolved, (unsigned)q2n);
+        if (nm) atomicAdd(cnt_near, (unsigned)__popc(nm));
+    }
+    __syncwarp();
+}
+
+// Focal agent of a warp: float32 state plus cos/sin(theta) in double-float (FP32 pipe only).
+template <bool HETERO>
+__device__ __forceinline__ FocalDev load_focal(const StepArgs &a, int i) {
+    FocalDev f;
+    f.x = a.x[i];
+    f.y = a.y[i];
+    f.r = HETERO ? a.radius[i] : a.radius0;
+    f.invr = 1.f / f.r;
+    df_sincos(a.th[i], c_sincos, f.cd, f.sd);
+    f.c = f.cd.hi + f.cd.lo;
+    f.s = f.sd.hi + f.sd.lo;
+    return f;
+}
+
+// Phase A for one lane's neighbour: the exact-zero / cull test of vf_supcalc.py:57-58 and
+// h = 0 (projections narrower than 2 pixels never fill anything).
+template <bool TORUS, bool HETERO>
+__device__ __forceinline__ bool candidate_live(const FocalDev &f, float xj, float yj, float rj,
+                                               bool valid, float cull_r2, const StepArgs &a) {
+    float dx, dy;
+    pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
+    const float d2 = fmaf(dx, dx, dy * dy);
+    if (HETERO) {
+        const bool same = (xj == f.x) && (yj == f.y);
+        return valid && !same && d2 <= rj * rj * a.g.cull;
+    }
+    return valid && d2 > 0.f && d2 <= cull_r2;   // equal radii: same position <=> zero offset
+}
+
+// Append the lane's live candidate to the warp queue; run phase B on every full batch of 32.
+template <bool TORUS, bool HETERO>
+__device__ __forceinline__ void enqueue_candidate(const FocalDev &f, bool live, float xj, float yj,
+                                                  float rj, QEntry<HETERO> *q, int &qn,
+                                                  QEntry<HETERO> *q2, int &q2n, uint32_t *vb,
+                                                  const StepArgs &a, unsigned *counters) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lm = __ballot_sync(ABM_FULL_MASK, live);
+    if (live) q[qn + __popc(lm & ((1u << lane) - 1u))] = QEntry<HETERO>::make(xj, yj, rj);
+    qn += __popc(lm);
+    __syncwarp();
+    if (qn >= 32) {   // warp-uniform
+        qn -= 32;
+        process_candidates<TORUS, HETERO>(f, q + qn, 32, q2, q2n, vb, a, &counters[0],
+                                          &counters[1]);
+    }
+}
+
+// Warp epilogue of a focal agent: the integral sums and (optionally) the bitmask to global.
+__device__ __forceinline__ void store_agent(const StepArgs &a, int i, const uint32_t *vb) {
+    const int lane = threadIdx.x & 31;
+    long long bc, bs, ec, es;
+    warp_integrals(vb, a.g, bc, bs, ec, es);
+    if (lane == 0) {
+        longlong2 *dst = reinterpret_cast<longlong2 *>(a.sums + 4 * (size_t)i);
+        dst[0] = make_longlong2(bc, bs);
+        dst[1] = make_longlong2(ec, es);
+    }
+    if (a.bits) {
+        uint32_t *dst = a.bits + (size_t)i * a.g.words;
+        for (int w = lane; w < a.g.words; w += 32) dst[w] = vb[w];
+    }
+}
+
+__device__ __forceinline__ void flush_counters(const StepArgs &a, const unsigned *counters) {
+    if (!a.diag) return;
+    if (counters[0]) atomicAdd(&a.diag[ABM_DIAG_PAIRS_RESOLVED], (unsigned long long)counters[0]);
+    if (counters[1]) atomicAdd(&a.diag[ABM_DIAG_NEAR_BOUNDARY], (unsigned long long)counters[1]);
+    if (counters[2]) atomicAdd(&a.diag[ABM_DIAG_TIMEOUTS], (unsigned long long)counters[2]);
+}
+
+// ---------------------------------------------------------------------------- l1 form
+// One block = one focal agent, WPA warps share its bitmask and split its neighbours.
+static size_t l1_smem_bytes(int wpa, int words, bool hetero) {
+    const size_t qe = hetero ? 16 : 8;
+    size_t b = (size_t)words * sizeof(uint32_t);
+    b = (b + 15) & ~size_t(15);
+    b += (size_t)wpa * (kQueue + kQueue2) * qe;
+    return b + 16;
+}
+
+template <bool TORUS, bool HETERO, int WPA>
+__global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = a.n, words = a.g.words, i = blockIdx.x;
+    uint32_t *vb = reinterpret_cast<uint32_t *>(smem);
+    size_t off = ((size_t)words * 4 + 15) & ~size_t(15);
+    QEntry<HETERO> *q = reinterpret_cast<QEntry<HETERO> *>(smem + off) + warp * (kQueue + kQueue2);
+    QEntry<HETERO> *q2 = q + kQueue;
+    off += (size_t)WPA * (kQueue + kQueue2) * sizeof(QEntry<HETERO>);
+    unsigned *counters = reinterpret_cast<unsigned *>(smem + off);
+
+    for (int w = threadIdx.x; w < words; w += 32 * WPA) vb[w] = 0u;
+    if (threadIdx.x < 4) counters[threadIdx.x] = 0u;
+    const FocalDev f = load_focal<HETERO>(a, i);
+    const float cull_r2 = f.r * f.r * a.g.cull;
+    if (WPA > 1) __syncthreads(); else __syncwarp();
+
+    int qn = 0, q2n = 0;
+    constexpr int kStep = 32 * WPA;
+    int j = warp * 32 + lane;
+    float xn = f.x, yn = f.y, rn = f.r;
+    if (j < n) {
+        xn = __ldg(a.x + j);
+        yn = __ldg(a.y + j);
+        if (HETERO) rn = __ldg(a.radius + j);
+    }
+    for (int jb = warp * 32; jb < n; jb += kStep) {
+        const float xj = xn, yj = yn, rj = rn;
+        const bool valid = jb + lane < n;
+        const int jn = jb + kStep + lane;   // prefetch the next chunk through L1
+        if (jn < n) {
+            xn = __ldg(a.x + jn);
+            yn = __ldg(a.y + jn);
+            if (HETERO) rn = __ldg(a.radius + jn);
+        }
+        const bool live = candidate_live<TORUS, HETERO>(f, xj, yj, rj, valid, cull_r2, a);
+        enqueue_candidate<TORUS, HETERO>(f, live, xj, yj, rj, q, qn, q2, q2n, vb, a, counters);
+    }
+    if (qn > 0) process_candidates<TORUS, HETERO>(f, q, qn, q2, q2n, vb, a, &counters[0],
+                                                  &counters[1]);
+    drain_deferred<TORUS, HETERO>(f, q2, q2n, vb, a, &counters[0], &counters[1]);
+    if (WPA > 1) __syncthreads(); else __syncwarp();
+    if (warp == 0) {
+        store_agent(a, i, vb);
+        if (lane == 0) flush_counters(a, counters);
+    }
+}
+
+// ---------------------------------------------------------------------------- tiled form
+// Several focal warps per block; neighbour tiles staged in shared memory by the TMA bulk
+// engine (double-buffered when the swarm spans more than one tile).
+static int tile_buffers(int n, int tile) { return n > tile ? 2 : 1; }
+
+static size_t tiled_smem_bytes(int warps, int tile, int words, bool hetero, int nbuf) {
     const int nf = hetero ? 3 : 2;
-    return 16 + 2 * (size_t)nf * tile * sizeof(float) + (size_t)warps * words * sizeof(uint32_t);
+    const size_t qe = hetero ? 16 : 8;
+    size_t b = 16 + (size_t)nbuf * nf * tile * sizeof(float);
+    b += (size_t)warps * words * sizeof(uint32_t);
+    b = (b + 15) & ~size_t(15);
+    b += (size_t)warps * (kQueue + kQueue2) * qe;
+    b += 16;  // block counters
+    return b;
 }
 
 template <bool TORUS, bool HETERO, bool TMA>
-__global__ void __launch_bounds__(1024) vpf_flock_step_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    const int tile = a.tile, n = a.n;
+    const int tile = a.tile, n = a.n, words = a.g.words;
     constexpr int NF = HETERO ? 3 : 2;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     float *buf0 = reinterpret_cast<float *>(smem + 16);
-    uint32_t *vb = reinterpret_cast<uint32_t *>(buf0 + 2 * NF * tile) + warp * a.g.words;
+    const int nbuf = n > tile ? 2 : 1;   // tile_buffers()
+    uint32_t *vball = reinterpret_cast<uint32_t *>(buf0 + nbuf * NF * tile);
+    uint32_t *vb = vball + warp * words;
+    size_t off = 16 + (size_t)nbuf * NF * tile * sizeof(float) + (size_t)nw * words * 4;
+    off = (off + 15) & ~size_t(15);
+    QEntry<HETERO> *q = reinterpret_cast<QEntry<HETERO> *>(smem + off) + warp * (kQueue + kQueue2);
+    QEntry<HETERO> *q2 = q + kQueue;
+    off += (size_t)nw * (kQueue + kQueue2) * sizeof(QEntry<HETERO>);
+    unsigned *counters = reinterpret_cast<unsigned *>(smem + off);
+
     const int i = blockIdx.x * nw + warp;
     const bool active = i < n;
-
-    FocalDev f;
-    double thd = 0.0;
-    if (active) {
-        f.x = a.x[i];
-        f.y = a.y[i];
-        f.r = HETERO ? a.radius[i] : a.radius0;
-        thd = (double)a.th[i];
-    } else {
-        f.x = f.y = 0.f;
-        f.r = a.radius0;
-    }
-    f.invr = 1.f / f.r;
-    double sn, cs;
-    sincos(thd, &sn, &cs);
-    f.c = (float)cs;
-    f.s = (float)sn;
-    f.cd = df_split(cs);
-    f.sd = df_split(sn);
-    for (int w = lane; w < a.g.words; w += 32) vb[w] = 0u;
-
+    if (tid < 4) counters[tid] = 0u;
+    for (int w = lane; w < words; w += 32) vb[w] = 0u;
     if (TMA && tid == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         fence_barrier_init();
     }
+    const FocalDev f = load_focal<HETERO>(a, active ? i : blockIdx.x * nw);
+    const float cull_r2 = f.r * f.r * a.g.cull;
     __syncthreads();
 
     const int ntiles = (n + tile - 1) / tile;
@@ -86,7 +378,7 @@ __global__ void __launch_bounds__(1024) vpf_flock_step_kernel(const StepArgs a) 
         const int tn = min(tile, n - base);
         const int tn4 = tn & ~3;
         if (tn4 > 0) {
-            float *dst = buf0 + (k & 1) * NF * tile;
+            float *dst = buf0 + (k & 1) * (nbuf - 1) * NF * tile;
             const uint32_t bytes = (uint32_t)tn4 * 4u;
             fence_proxy_async();
             mbar_expect_tx(&bars[k & 1], bytes * NF);
@@ -97,22 +389,24 @@ __global__ void __launch_bounds__(1024) vpf_flock_step_kernel(const StepArgs a) 
     };
     if (TMA && tid == 0) issue(0);
 
+    int qn = 0, q2n = 0;
     for (int k = 0; k < ntiles; ++k) {
         const int base = k * tile;
         const int tn = min(tile, n - base);
-        int tn_s;   // neighbours of this tile that are in shared memory
-        float *cur = buf0 + (k & 1) * NF * tile;
+        int tn_s;
+        const float *cur = buf0 + (k & 1) * (nbuf - 1) * NF * tile;
         if (TMA) {
             if (tid == 0 && k + 1 < ntiles) issue(k + 1);
             tn_s = tn & ~3;
             if (tn_s > 0 && !mbar_wait(&bars[k & 1], (uint32_t)((k >> 1) & 1))) {
-                if (a.diag && lane == 0) atomicAdd(&a.diag[ABM_DIAG_TIMEOUTS], 1ull);
+                if (lane == 0) atomicAdd(&counters[2], 1u);
             }
         } else {
-            for (int q = tid; q < tn; q += blockDim.x) {
-                cur[q] = a.x[base + q];
-                cur[tile + q] = a.y[base + q];
-                if (HETERO) cur[2 * tile + q] = a.radius[base + q];
+            float *w = buf0 + (k & 1) * (nbuf - 1) * NF * tile;
+            for (int qi = tid; qi < tn; qi += blockDim.x) {
+                w[qi] = a.x[base + qi];
+                w[tile + qi] = a.y[base + qi];
+                if (HETERO) w[2 * tile + qi] = a.radius[base + qi];
             }
             tn_s = tn;
             __syncthreads();
@@ -131,70 +425,97 @@ __global__ void __launch_bounds__(1024) vpf_flock_step_kernel(const StepArgs a) 
                     yj = a.y[base + jj];
                     if (HETERO) rj = a.radius[base + jj];
                 }
-                int s, e;
-                bool vis;
-                pair_projection<TORUS, HETERO>(f, xj, yj, rj, HETERO ? rcp_approx(rj) : f.invr,
-                                               valid, a.g, a.W, a.H, s, e, vis, a.diag);
-                if (vis) raster_projection(vb, a.g.rv, s, e);
+                const bool live = candidate_live<TORUS, HETERO>(f, xj, yj, rj, valid, cull_r2, a);
+                enqueue_candidate<TORUS, HETERO>(f, live, xj, yj, rj, q, qn, q2, q2n, vb, a,
+                                                 counters);
             }
         }
         __syncthreads();
     }
-    if (!active) return;
+    if (active) {
+        if (qn > 0) process_candidates<TORUS, HETERO>(f, q, qn, q2, q2n, vb, a, &counters[0],
+                                                      &counters[1]);
+        drain_deferred<TORUS, HETERO>(f, q2, q2n, vb, a, &counters[0], &counters[1]);
+        __syncwarp();
+        store_agent(a, i, vb);
+    }
+    __syncthreads();
+    if (tid == 0) flush_counters(a, counters);
+}
 
-    long long bc, bs, ec, es;
-    warp_integrals(vb, a.g, bc, bs, ec, es);
-    if (a.bits) {
-        uint32_t *dst = a.bits + (size_t)i * a.g.words;
-        for (int w = lane; w < a.g.words; w += 32) dst[w] = vb[w];
+// Evaluates the in-kernel double-float cos/sin (verification hook for the tests).
+__global__ void check_sincos_kernel(const float *theta, int n, double *out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dfl c, s;
+    df_sincos(theta[k], c_sincos, c, s);
+    out[2 * k] = (double)c.hi + (double)c.lo;
+    out[2 * k + 1] = (double)s.hi + (double)s.lo;
+}
+
+// ---------------------------------------------------------------------------- update
+// One thread per agent: VSWRM combination (vf_supcalc.py:233-254) and the state update.
+__global__ void __launch_bounds__(128) vpf_update_kernel(const StepArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const UpdateParams &p = a.up;
+    const longlong2 s0 = reinterpret_cast<const longlong2 *>(a.sums)[2 * (size_t)k];
+    const longlong2 s1 = reinterpret_cast<const longlong2 *>(a.sums)[2 * (size_t)k + 1];
+    const double alp0 = a.alp0 ? (double)a.alp0[k] : p.alp0;
+    const double bet0 = a.bet0 ? (double)a.bet0[k] : p.bet0;
+    const double v0 = a.v0 ? (double)a.v0[k] : p.v0;
+    const double R = a.radius ? (double)a.radius[k] : (double)a.radius0;
+    double vel = (double)a.v[k];
+    double ab = 0, ae = 0, bb = 0, be = 0, dv = 0, dpsi = 0;
+    if (a.g.phi_ok) {
+        ab = alp0 * (-(double)s0.x * kInvFix);
+        ae = alp0 * p.alp1 * ((double)s1.x * kInvFix);
+        bb = bet0 * (-(double)s0.y * kInvFix);
+        be = bet0 * p.bet1 * ((double)s1.y * kInvFix);
+        dv = p.gam * (v0 - vel) + ab + ae;
+        dpsi = bb + be;
     }
-    if (lane == 0) {
-        const UpdateParams &p = a.up;
-        const double alp0 = a.alp0 ? (double)a.alp0[i] : p.alp0;
-        const double bet0 = a.bet0 ? (double)a.bet0[i] : p.bet0;
-        const double v0 = a.v0 ? (double)a.v0[i] : p.v0;
-        double vel = (double)a.v[i];
-        double ab = 0, ae = 0, bb = 0, be = 0, dv = 0, dpsi = 0;
-        if (a.g.phi_ok) {
-            ab = alp0 * (-(double)bc * kInvFix);
-            ae = alp0 * p.alp1 * ((double)ec * kInvFix);
-            bb = bet0 * (-(double)bs * kInvFix);
-            be = bet0 * p.bet1 * ((double)es * kInvFix);
-            dv = p.gam * (v0 - vel) + ab + ae;
-            dpsi = bb + be;
-        }
-        if (a.terms) {
-            double *t = a.terms + 6 * (size_t)i;
-            t[0] = dv;
-            t[1] = dpsi;
-            t[2] = ab;
-            t[3] = ae;
-            t[4] = bb;
-            t[5] = be;
-        }
-        double x = (double)f.x, y = (double)f.y, th = thd;
-        update_agent(p, (double)f.r, dpsi, dv, x, y, th, vel);
-        a.xo[i] = (float)x;
-        a.yo[i] = (float)y;
-        a.tho[i] = (float)th;
-        a.vo[i] = (float)vel;
-        if (a.diag && !(isfinite(x) && isfinite(y) && isfinite(th) && isfinite(vel)))
-            atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
+    if (a.terms) {
+        double *t = a.terms + 6 * (size_t)k;
+        t[0] = dv;
+        t[1] = dpsi;
+        t[2] = ab;
+        t[3] = ae;
+        t[4] = bb;
+        t[5] = be;
     }
+    double x = (double)a.x[k], y = (double)a.y[k], th = (double)a.th[k];
+    update_agent(p, R, dpsi, dv, x, y, th, vel);
+    a.xo[k] = (float)x;
+    a.yo[k] = (float)y;
+    a.tho[k] = (float)th;
+    a.vo[k] = (float)vel;
+    if (a.diag && !(isfinite(x) && isfinite(y) && isfinite(th) && isfinite(vel)))
+        atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
+}
+
+template <bool TORUS, bool HETERO>
+static int launch_l1(const StepArgs &a, int wpa, cudaStream_t stream) {
+    const size_t smem = l1_smem_bytes(wpa, a.g.words, HETERO);
+    if (wpa == 1) vpf_pairs_l1_kernel<TORUS, HETERO, 1><<<a.n, 32, smem, stream>>>(a);
+    else if (wpa == 2) vpf_pairs_l1_kernel<TORUS, HETERO, 2><<<a.n, 64, smem, stream>>>(a);
+    else vpf_pairs_l1_kernel<TORUS, HETERO, 4><<<a.n, 128, smem, stream>>>(a);
+    return check_cuda(cudaGetLastError(), "vpf_pairs_l1_kernel launch");
 }
 
 template <bool TORUS, bool HETERO, bool TMA>
-static int launch_step(const StepArgs &a, int warps, cudaStream_t stream) {
-    auto kern = vpf_flock_step_kernel<TORUS, HETERO, TMA>;
+static int launch_tiled(const StepArgs &a, int warps, cudaStream_t stream) {
+    auto kern = vpf_pairs_tiled_kernel<TORUS, HETERO, TMA>;
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    const size_t smem = step_smem_bytes(warps, a.tile, a.g.words, HETERO);
+    const size_t smem = tiled_smem_bytes(warps, a.tile, a.g.words, HETERO,
+                                         tile_buffers(a.n, a.tile));
     const int blocks = (a.n + warps - 1) / warps;
     kern<<<blocks, warps * 32, smem, stream>>>(a);
-    return check_cuda(cudaGetLastError(), "vpf_flock_step_kernel launch");
+    return check_cuda(cudaGetLastError(), "vpf_pairs_tiled_kernel launch");
 }
 
 static bool aligned16(const void *p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; }
@@ -295,10 +616,14 @@ __global__ void project_pairs_kernel(const ProjArgs a) {
         unc_t = unc_h = false;
     }
     if (unc_t || unc_h) {
-        int2 th = resolve_pair(f.cd, f.sd, ex, ey, rj, resolve_grid(g), unc_t, unc_h, u, ps2, t,
-                               h, a.diag);
+        int3 th = resolve_pair(f.cd, f.sd, ex, ey, rj, resolve_grid(g), unc_t, unc_h, u, ps2, t,
+                               h);
         t = th.x;
         h = th.y;
+        if (a.diag) {
+            atomicAdd(&a.diag[ABM_DIAG_PAIRS_RESOLVED], 1ull);
+            if (th.z) atomicAdd(&a.diag[ABM_DIAG_NEAR_BOUNDARY], 1ull);
+        }
     }
     int s = t - h, e = t + h;
     const int rv = g.rv;
@@ -393,6 +718,23 @@ int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile) {
     return ABM_OK;
 }
 
+int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent) {
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    if (mode < 0 || mode > 2) return set_error(ABM_ERR_INVALID_ARG, "mode=%d", mode);
+    if (warps_per_agent && warps_per_agent != 1 && warps_per_agent != 2 && warps_per_agent != 4)
+        return set_error(ABM_ERR_INVALID_ARG, "warps_per_agent=%d", warps_per_agent);
+    g_mode = mode;
+    if (warps_per_agent) g_wpa = warps_per_agent;
+    return ABM_OK;
+}
+
+int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent) {
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    if (mode) *mode = g_mode;
+    if (warps_per_agent) *warps_per_agent = g_wpa;
+    return ABM_OK;
+}
+
 int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
                        const abm_vf_params *p, const abm_agent_overrides *ov,
                        uint32_t *vpf_bits_dev, double *terms_dev,
@@ -410,8 +752,13 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
         return set_error(ABM_ERR_INVALID_ARG, "%s: out must not alias in", fn);
     const GridDev *g = grid_for(p->rv, p->fov0, p->fov1, &st);
     if (!g) return st;
-    int warps, tile;
+    if ((st = ensure_sincos_table())) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    long long *sums = (long long *)workspace(s, 32 * (size_t)n, &st);
+    if (!sums) return st;
+    int warps, tile, mode, wpa;
     abm_vpf_get_step_config(&warps, &tile);
+    abm_vpf_get_step_mode(&mode, &wpa);
     StepArgs a;
     memset(&a, 0, sizeof(a));
     a.x = in->x;
@@ -427,16 +774,6 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     a.bet0 = ov ? ov->bet0 : nullptr;
     a.v0 = ov ? ov->v0 : nullptr;
     a.n = n;
-    a.tile = std::min(tile, ((n + 31) / 32) * 32);
-    {   // keep the tiles + bitmasks within the 200 KiB of dynamic shared memory we opt into
-        const size_t words_bytes = (size_t)warps * g->words * sizeof(uint32_t);
-        const int nf = (ov && ov->radius) ? 3 : 2;
-        const long fit = ((long)(200 * 1024) - 16 - (long)words_bytes) / (2L * nf * 4);
-        if (fit < 32)
-            return set_error(ABM_ERR_UNSUPPORTED, "%s: rv=%d too large for %d warps per block",
-                             fn, p->rv, warps);
-        a.tile = std::min<int>(a.tile, (int)(fit / 32) * 32);
-    }
     a.radius0 = (float)p->radius;
     a.bits = vpf_bits_dev;
     a.terms = terms_dev;
@@ -445,20 +782,51 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     a.H = {(float)p->height, (float)(p->height - (double)(float)p->height)};
     a.up = make_update(p);
     a.g = *g;
+    a.sums = sums;
     const bool torus = p->boundary == ABM_BOUNDARY_INFINITE;
     const bool hetero = a.radius != nullptr;
-    const bool tma = aligned16(a.x) && aligned16(a.y) && aligned16(a.radius);
-    cudaStream_t s = (cudaStream_t)stream;
-    if (!torus && !hetero) st = tma ? launch_step<false, false, true>(a, warps, s)
-                                     : launch_step<false, false, false>(a, warps, s);
-    else if (!torus && hetero) st = tma ? launch_step<false, true, true>(a, warps, s)
-                                         : launch_step<false, true, false>(a, warps, s);
-    else if (torus && !hetero) st = tma ? launch_step<true, false, true>(a, warps, s)
-                                         : launch_step<true, false, false>(a, warps, s);
-    else st = tma ? launch_step<true, true, true>(a, warps, s)
-                  : launch_step<true, true, false>(a, warps, s);
+    // auto: the l1 form while the positions fit comfortably in L1, tiled beyond
+    const bool use_l1 = mode == 1 || (mode == 0 && n <= 16384);
+    if (use_l1) {
+        if (!torus && !hetero) st = launch_l1<false, false>(a, wpa, s);
+        else if (!torus && hetero) st = launch_l1<false, true>(a, wpa, s);
+        else if (torus && !hetero) st = launch_l1<true, false>(a, wpa, s);
+        else st = launch_l1<true, true>(a, wpa, s);
+    } else {
+        a.tile = std::min(tile, ((n + 31) / 32) * 32);
+        const long per = (hetero ? 3L : 2L) * 4L;   // bytes per staged neighbour
+        const long room = (long)(200 * 1024) - (long)tiled_smem_bytes(warps, 0, g->words, hetero, 1);
+        if (room < 2 * 32 * per)
+            return set_error(ABM_ERR_UNSUPPORTED, "%s: rv=%d too large for %d warps per block",
+                             fn, p->rv, warps);
+        int t = a.tile;
+        if (t >= n && (long)t * per > room) t = (int)((room / per) / 32 * 32);
+        if (t < n && 2L * t * per > room) t = (int)((room / (2 * per)) / 32 * 32);
+        a.tile = t;
+        const bool tma = aligned16(a.x) && aligned16(a.y) && aligned16(a.radius);
+        if (!torus && !hetero) st = tma ? launch_tiled<false, false, true>(a, warps, s)
+                                         : launch_tiled<false, false, false>(a, warps, s);
+        else if (!torus && hetero) st = tma ? launch_tiled<false, true, true>(a, warps, s)
+                                             : launch_tiled<false, true, false>(a, warps, s);
+        else if (torus && !hetero) st = tma ? launch_tiled<true, false, true>(a, warps, s)
+                                             : launch_tiled<true, false, false>(a, warps, s);
+        else st = tma ? launch_tiled<true, true, true>(a, warps, s)
+                      : launch_tiled<true, true, false>(a, warps, s);
+    }
     if (st) return st;
+    vpf_update_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+    if ((st = check_cuda(cudaGetLastError(), "vpf_update_kernel launch"))) return st;
     return g->phi_ok ? ABM_OK : ABM_WARN_PHI_MISMATCH;
+}
+
+int abm_vpf_check_sincos(const float *theta_dev, int32_t n, double *out_dev, void *stream) {
+    if (n < 0 || (n > 0 && (!theta_dev || !out_dev)))
+        return set_error(ABM_ERR_INVALID_ARG, "abm_vpf_check_sincos: bad arguments");
+    if (n == 0) return ABM_OK;
+    int st = ensure_sincos_table();
+    if (st) return st;
+    check_sincos_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(theta_dev, n, out_dev);
+    return check_cuda(cudaGetLastError(), "check_sincos_kernel launch");
 }
 
 int abm_vpf_project_rows(const double fov[2], int32_t rv, const double pos_host[2],

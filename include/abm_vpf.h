@@ -27,8 +27,10 @@
  *     raw pixel k, i.e. the pixel order VSWRM integrates (np.flip of the reference's
  *     returned/stored soc_v_field).  Bits >= Rv are zero.
  *   - The library allocates device memory only for its cached lookup tables (one set per
- *     distinct grid: Rv and field of view); the first call for a grid builds them
- *     synchronously, so make that call before capturing a CUDA graph.
+ *     distinct grid: Rv and field of view) and for a per-stream workspace of 32 bytes per
+ *     agent that abm_vpf_flock_step uses between its two launches; the first call for a grid,
+ *     and a call with more agents than the stream's workspace holds, allocate synchronously,
+ *     so make such a call before capturing a CUDA graph.
  */
 #ifndef ABM_VPF_H
 #define ABM_VPF_H
@@ -174,11 +176,26 @@ int abm_vswrm_integrals(int32_t n_fields, int32_t rv, const uint32_t *bits_dev,
 int abm_vpf_set_step_config(int32_t warps_per_block, int32_t tile);
 int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile);
 
+/* Form of the pair kernel of abm_vpf_flock_step: mode 0 = automatic (the L1 form up to 16384
+ * agents, the tiled form beyond), 1 = L1 form (one block per focal agent, neighbours read
+ * through the read-only L1 path), 2 = tiled form (warps_per_block focal agents share
+ * TMA-staged neighbour tiles).  warps_per_agent in {1, 2, 4} splits one focal agent's
+ * neighbours over that many warps in the L1 form; 0 keeps the current value.  All forms give
+ * bit-identical results. */
+int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent);
+int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent);
+
+/* Verification hook (no counterpart in the reference): evaluates the double-float cos/sin of
+ * float32 headings that the pair kernels use for the focal agent's heading vector.
+ * out_dev: n x 2 doubles (cos, sin). */
+int abm_vpf_check_sincos(const float *theta_dev, int32_t n, double *out_dev, void *stream);
+
 /* ---------------------------------------------------------------- measurement utilities */
 
 /* Pipe-throughput probe (no counterpart in the reference; used for the roofline
  * denominators): kind 0 launches independent FFMA chains, kind 1 independent MUFU.RSQ chains,
- * on blocks x threads threads for `iters` rounds.  *ops_out receives the number of FP32 ops
+ * kind 2 independent packed FP32x2 FFMA2 chains, on blocks x threads threads for `iters`
+ * rounds.  *ops_out receives the number of FP32 ops
  * (an FFMA counts 2) or MUFU ops the launch performs; time it with CUDA events on `stream`.
  * sink_dev: >= threads floats of scratch that keeps the chains live. */
 int abm_probe_pipe_peak(int32_t kind, int32_t blocks, int32_t threads, int32_t iters,

@@ -159,7 +159,9 @@ def test_permutation_invariance_full_size():
 
 
 def test_launch_configs_agree():
-    """Every (warps per block, tile) configuration gives bit-identical results."""
+    """Every kernel form and launch configuration gives bit-identical results: the L1 form
+    with 1, 2 and 4 warps per agent, and the TMA-tiled form with several (warps per block,
+    tile) shapes including multi-tile double buffering."""
     from abm_gb300 import _lib
     from abm_gb300.params import VFParams
     from abm_gb300.swarm import VFSwarm
@@ -168,18 +170,40 @@ def test_launch_configs_agree():
     vp = VFParams(width=2000.0, height=2000.0, rv=1200, radius=5.0)
     outs = []
     try:
-        for warps, tile in ((8, 2048), (4, 256), (16, 1024), (32, 64), (1, 4096)):
+        for mode, wpa, warps, tile in ((1, 1, 8, 8192), (1, 2, 8, 8192), (1, 4, 8, 8192),
+                                       (2, 1, 8, 2048), (2, 1, 4, 256), (2, 1, 16, 1024),
+                                       (2, 1, 32, 64), (2, 1, 1, 4096)):
+            _lib.check(lib.abm_vpf_set_step_mode(mode, wpa))
             _lib.check(lib.abm_vpf_set_step_config(warps, tile))
             s = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
             s.step(want_vpf=True, want_terms=True)
             outs.append((s.vpf_numpy(), s.terms.cpu().numpy(), s.state_numpy()))
     finally:
-        lib.abm_vpf_set_step_config(8, 2048)
+        lib.abm_vpf_set_step_mode(0, 1)
+        lib.abm_vpf_set_step_config(8, 8192)
     for o in outs[1:]:
         assert np.array_equal(o[0], outs[0][0])
         assert np.array_equal(o[1], outs[0][1])
         for k in o[2]:
             assert np.array_equal(o[2][k], outs[0][2][k])
+
+
+def test_double_float_sincos():
+    """The FP32-only double-float cos/sin of the focal heading is within 1e-13 of FP64."""
+    import ctypes
+    import torch
+    from abm_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(1)
+    th = np.concatenate([rng.uniform(0, 2 * np.pi, 200000), rng.uniform(-7, 14, 20000),
+                         np.arange(0, 1025) * (2 * np.pi / 1024)]).astype(np.float32)
+    t = torch.as_tensor(th, device="cuda")
+    out = torch.empty((len(th), 2), dtype=torch.float64, device="cuda")
+    _lib.check(lib.abm_vpf_check_sincos(_lib.fptr(t), len(th), _lib.dptr(out), None))
+    o = out.cpu().numpy()
+    th64 = th.astype(np.float64)
+    assert np.max(np.abs(o[:, 0] - np.cos(th64))) < 1e-13
+    assert np.max(np.abs(o[:, 1] - np.sin(th64))) < 1e-13
 
 
 def test_unaligned_state_uses_plain_loads():
@@ -188,16 +212,24 @@ def test_unaligned_state_uses_plain_loads():
     import torch
     from abm_gb300.params import VFParams
     from abm_gb300.swarm import VFSwarm
+    from abm_gb300 import _lib
+    lib = _lib.load()
     st = seeded_swarm(9, 777, 1500.0, 1500.0)
     vp = VFParams(width=1500.0, height=1500.0, rv=1200)
-    a = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
-    a.step(want_vpf=True)
-    b = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
-    for k in ("x", "y"):
-        big = torch.zeros(b.n + 1, dtype=torch.float32, device="cuda")
-        big[1:] = b._cur[k]
-        b._cur[k] = big[1:]          # 4-byte offset: not 16-byte aligned
-    b.step(want_vpf=True)
+    try:
+        _lib.check(lib.abm_vpf_set_step_mode(2, 0))
+        _lib.check(lib.abm_vpf_set_step_config(8, 256))
+        a = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+        a.step(want_vpf=True)
+        b = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+        for k in ("x", "y"):
+            big = torch.zeros(b.n + 1, dtype=torch.float32, device="cuda")
+            big[1:] = b._cur[k]
+            b._cur[k] = big[1:]          # 4-byte offset: not 16-byte aligned
+        b.step(want_vpf=True)
+    finally:
+        lib.abm_vpf_set_step_mode(0, 1)
+        lib.abm_vpf_set_step_config(8, 8192)
     assert np.array_equal(a.vpf_numpy(), b.vpf_numpy())
 
 
