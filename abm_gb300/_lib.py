@@ -30,6 +30,8 @@ ABM_ERR_NONFINITE = -5
 ABM_ERR_UNSUPPORTED = -6
 ABM_ERR_NO_DEVICE = -7
 ABM_MAX_RV = 16384
+ABM_NOALLOC_MAX_AGENTS = 65536
+ABM_NOALLOC_MAX_RV = 8192
 ABM_DIAG_COUNT = 8
 DIAG_PAIRS_RESOLVED, DIAG_NEAR_BOUNDARY, DIAG_NONFINITE, DIAG_TIMEOUTS = 0, 1, 2, 3
 
@@ -61,6 +63,10 @@ SIGNATURES = [
     ("abm_phi_table", c_int32, [c_int32, c_double_p, c_int32]),
     ("abm_vpf_words", c_int32, [c_int32]),
     ("abm_vpf_flock_step", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
+      ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_u32_p, c_double_p,
+      c_u64_p, c_void_p]),
+    ("abm_vpf_flock_step_noalloc", c_int32,
      [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
       ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_u32_p, c_double_p,
       c_u64_p, c_void_p]),

@@ -119,6 +119,56 @@ struct QEntry<true> {
     }
 };
 
+// ---------------------------------------------------------------------------- no-alloc scratch
+// Scratch of abm_vpf_flock_step_noalloc, for callers that cannot allocate device memory:
+// the per-agent sums (32 B x kNoAllocMaxAgents) and one grid's lookup tables (Rv up to
+// kNoAllocMaxRv), carved out of one file-scope array that every GPU loading the library holds
+// until the process exits (about 2.5 MiB).
+constexpr int kNoAllocMaxAgents = 65536;
+constexpr int kNoAllocMaxRv = 8192;
+constexpr size_t kNaAlign = 256;
+constexpr size_t na_round(size_t b) { return (b + kNaAlign - 1) & ~(kNaAlign - 1); }
+constexpr size_t kNaSums = 0;
+constexpr size_t kNaMid = kNaSums + na_round(32ull * kNoAllocMaxAgents);
+constexpr size_t kNaCot2 = kNaMid + na_round(sizeof(float4) * kNoAllocMaxRv);
+constexpr size_t kNaQ = kNaCot2 + na_round(sizeof(float2) * (kNoAllocMaxRv / 4 + 2));
+constexpr size_t kNaCpt = kNaQ + na_round(sizeof(longlong2) * (kNoAllocMaxRv + 1));
+constexpr size_t kNaBytes = kNaCpt + na_round(sizeof(longlong2) * kNoAllocMaxRv);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+struct NoAllocDevice {
+    unsigned char *base = nullptr;   // device address of g_noalloc_scratch on this device
+    bool grid_loaded = false;        // which grid's tables the array holds
+    int rv = 0;
+    double fov0 = 0, fov1 = 0;
+    GridDev g;
+};
+
+// Once per device (with that device current): the device address of the scratch array.
+static NoAllocDevice *noalloc_device(int *status) {
+    static std::mutex mu;
+    static NoAllocDevice devs[64];
+    int dev = 0;
+    *status = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (*status) return nullptr;
+    if (dev < 0 || dev >= 64) {
+        *status = set_error(ABM_ERR_UNSUPPORTED, "device %d beyond the no-alloc table", dev);
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    NoAllocDevice &d = devs[dev];
+    if (!d.base) {
+        void *ptr = nullptr;
+        *status = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_scratch),
+                             "cudaGetSymbolAddress(g_noalloc_scratch)");
+        if (*status) return nullptr;
+        d.base = (unsigned char *)ptr;
+    }
+    *status = ABM_OK;
+    return &d;
+}
+
 // Heavy decision + rasterisation of up to 32 queued candidates (lane < cnt holds one).
 template <bool TORUS, bool HETERO>
 __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEntry<HETERO> *q,
@@ -735,27 +785,13 @@ int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent) {
     return ABM_OK;
 }
 
-int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
+// Launches of one step (pair kernel + update kernel) given the grid tables and the sums
+// buffer; shared by abm_vpf_flock_step and abm_vpf_flock_step_noalloc.
+static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
                        const abm_vf_params *p, const abm_agent_overrides *ov,
-                       uint32_t *vpf_bits_dev, double *terms_dev,
-                       unsigned long long *diag_dev, void *stream) {
-    const char *fn = "abm_vpf_flock_step";
-    int st = validate_params(p, fn);
-    if (st) return st;
-    if (!in || !out) return set_error(ABM_ERR_INVALID_ARG, "%s: state is NULL", fn);
-    if (n < 0) return set_error(ABM_ERR_INVALID_ARG, "%s: n=%d", fn, n);
-    if (n == 0) return ABM_OK;
-    if (!in->x || !in->y || !in->theta || !in->v || !out->x || !out->y || !out->theta ||
-        !out->v)
-        return set_error(ABM_ERR_INVALID_ARG, "%s: a state array is NULL", fn);
-    if (in->x == out->x || in->y == out->y || in->theta == out->theta || in->v == out->v)
-        return set_error(ABM_ERR_INVALID_ARG, "%s: out must not alias in", fn);
-    const GridDev *g = grid_for(p->rv, p->fov0, p->fov1, &st);
-    if (!g) return st;
-    if ((st = ensure_sincos_table())) return st;
-    cudaStream_t s = (cudaStream_t)stream;
-    long long *sums = (long long *)workspace(s, 32 * (size_t)n, &st);
-    if (!sums) return st;
+                       uint32_t *vpf_bits_dev, double *terms_dev, unsigned long long *diag_dev,
+                       cudaStream_t s, const GridDev *g, long long *sums, const char *fn) {
+    int st;
     int warps, tile, mode, wpa;
     abm_vpf_get_step_config(&warps, &tile);
     abm_vpf_get_step_mode(&mode, &wpa);
@@ -817,6 +853,87 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     vpf_update_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
     if ((st = check_cuda(cudaGetLastError(), "vpf_update_kernel launch"))) return st;
     return g->phi_ok ? ABM_OK : ABM_WARN_PHI_MISMATCH;
+}
+
+static int step_validate(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
+                         const abm_vf_params *p, const char *fn) {
+    int st = validate_params(p, fn);
+    if (st) return st;
+    if (!in || !out) return set_error(ABM_ERR_INVALID_ARG, "%s: state is NULL", fn);
+    if (n < 0) return set_error(ABM_ERR_INVALID_ARG, "%s: n=%d", fn, n);
+    if (n == 0) return ABM_OK;
+    if (!in->x || !in->y || !in->theta || !in->v || !out->x || !out->y || !out->theta ||
+        !out->v)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: a state array is NULL", fn);
+    if (in->x == out->x || in->y == out->y || in->theta == out->theta || in->v == out->v)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: out must not alias in", fn);
+    return ABM_OK;
+}
+
+int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
+                       const abm_vf_params *p, const abm_agent_overrides *ov,
+                       uint32_t *vpf_bits_dev, double *terms_dev,
+                       unsigned long long *diag_dev, void *stream) {
+    const char *fn = "abm_vpf_flock_step";
+    int st = step_validate(in, out, n, p, fn);
+    if (st || n == 0) return st;
+    const GridDev *g = grid_for(p->rv, p->fov0, p->fov1, &st);
+    if (!g) return st;
+    if ((st = ensure_sincos_table())) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    long long *sums = (long long *)workspace(s, 32 * (size_t)n, &st);
+    if (!sums) return st;
+    return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, g, sums, fn);
+}
+
+int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
+                               const abm_vf_params *p, const abm_agent_overrides *ov,
+                               uint32_t *vpf_bits_dev, double *terms_dev,
+                               unsigned long long *diag_dev, void *stream) {
+    const char *fn = "abm_vpf_flock_step_noalloc";
+    int st = step_validate(in, out, n, p, fn);
+    if (st || n == 0) return st;
+    if (n > kNoAllocMaxAgents)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: n=%d exceeds the no-alloc maximum of %d agents",
+                         fn, n, kNoAllocMaxAgents);
+    if (p->rv > kNoAllocMaxRv)
+        return set_error(ABM_ERR_RV, "%s: rv=%d exceeds the no-alloc maximum of %d pixels", fn,
+                         p->rv, kNoAllocMaxRv);
+    NoAllocDevice *d = noalloc_device(&st);
+    if (!d) return st;
+    if ((st = ensure_sincos_table())) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!d->grid_loaded || d->rv != p->rv || d->fov0 != p->fov0 || d->fov1 != p->fov1) {
+        // (re)load this grid's tables into the array, ordered on the caller's stream
+        GridHostTables t;
+        build_grid_host(p->rv, p->fov0, p->fov1, t);
+        GridDev g = t.g;
+        g.mid = (const float4 *)(d->base + kNaMid);
+        g.cot2 = (const float2 *)(d->base + kNaCot2);
+        g.q = (const longlong2 *)(d->base + kNaQ);
+        g.cpt = (const longlong2 *)(d->base + kNaCpt);
+        const struct { size_t off; const void *src; size_t bytes; } parts[] = {
+            {kNaMid, t.mid.data(), t.mid.size() * sizeof(float)},
+            {kNaCot2, t.cot2.data(), t.cot2.size() * sizeof(float)},
+            {kNaQ, t.q.data(), t.q.size() * sizeof(long long)},
+            {kNaCpt, t.cpt.data(), t.cpt.size() * sizeof(long long)}};
+        for (const auto &pt : parts) {
+            st = check_cuda(cudaMemcpyAsync(d->base + pt.off, pt.src, pt.bytes,
+                                            cudaMemcpyHostToDevice, s),
+                            "cudaMemcpyAsync(no-alloc tables)");
+            if (st) {
+                d->grid_loaded = false;
+                return st;
+            }
+        }
+        d->g = g;
+        d->rv = p->rv;
+        d->fov0 = p->fov0;
+        d->fov1 = p->fov1;
+        d->grid_loaded = true;
+    }
+    return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, &d->g,
+                       (long long *)(d->base + kNaSums), fn);
 }
 
 int abm_vpf_check_sincos(const float *theta_dev, int32_t n, double *out_dev, void *stream) {

@@ -144,6 +144,30 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
                        unsigned long long *diag_dev, void *stream);
 
 /*
+ * Allocation-free variant of abm_vpf_flock_step (no counterpart in the reference): the same
+ * step, arguments, results and status codes, for callers that cannot call cudaMalloc, such as
+ * code running inside another framework's memory pool, a host that has reserved all device
+ * memory, or a graph-building layer that must not change the allocation state.  Its scratch
+ * (the per-agent VSWRM sums between the two launches, and the lookup tables of one grid) lives
+ * in a file-scope device array of about 2.5 MiB that every GPU loading the library holds until
+ * the process exits; no cudaMalloc, cudaFree or other allocating routine is called.
+ * Limits: n <= ABM_NOALLOC_MAX_AGENTS and rv <= ABM_NOALLOC_MAX_RV, larger values return
+ * ABM_ERR_INVALID_ARG / ABM_ERR_RV with a message.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and uploads the grid tables, and a call with a
+ * different rv or field of view uploads them again (synchronously from pageable memory), so
+ * make the first call, and the first call for each grid, before any stream capture.  Every
+ * call shares the one array and it keeps the last call's contents (nothing in it needs to
+ * start at zero: each launch overwrites the sums it reads); calls that overlap on the GPU
+ * race on it, so serialise them.
+ */
+#define ABM_NOALLOC_MAX_AGENTS 65536
+#define ABM_NOALLOC_MAX_RV 8192
+int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
+                               const abm_vf_params *p, const abm_agent_overrides *ov,
+                               uint32_t *vpf_bits_dev, double *terms_dev,
+                               unsigned long long *diag_dev, void *stream);
+
+/*
  * Drop-in twin of vf_supcalc.projection_field (vf_supcalc.py:20-138): the dense per-object
  * rows of one focal agent, flipped like the reference's return value.
  * pos_host: focal top-left (x, y) in double; obj_xy_dev: n_obj * 2 doubles (device);
