@@ -66,6 +66,10 @@ SIGNATURES = [
      [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
       ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_u32_p, c_double_p,
       c_u64_p, c_void_p]),
+    ("abm_vpf_flock_batched", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32, c_i32_p, c_i32_p,
+      c_i32_p, ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_u32_p,
+      c_double_p, c_u64_p, c_void_p]),
     ("abm_vpf_flock_step_noalloc", c_int32,
      [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
       ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_u32_p, c_double_p,
@@ -145,6 +149,12 @@ def u32ptr(t):
     if t is None:
         return None
     return ctypes.cast(t.data_ptr(), c_u32_p)
+
+
+def i32ptr(t):
+    if t is None:
+        return None
+    return ctypes.cast(t.data_ptr(), c_i32_p)
 
 
 def u64ptr(t):

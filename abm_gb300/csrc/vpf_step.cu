@@ -36,6 +36,9 @@ struct StepArgs {
     UpdateParams up;
     GridDev g;
     long long *sums;       // n x 4 workspace: bc, bs, ec, es of every agent
+    // batched sweeps: agent i sees the agents [seg_begin[i], seg_end[i]) of its instance;
+    // block b works on agent order[b] (largest instances first); all NULL for one swarm
+    const int *seg_begin, *seg_end, *order;
 };
 
 static int g_warps = 8;    // tiled form: focal warps per block
@@ -330,7 +333,10 @@ template <bool TORUS, bool HETERO, int WPA>
 __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int n = a.n, words = a.g.words, i = blockIdx.x;
+    const int words = a.g.words;
+    const int i = a.order ? a.order[blockIdx.x] : blockIdx.x;
+    const int j0 = a.seg_begin ? a.seg_begin[i] : 0;
+    const int n = a.seg_end ? a.seg_end[i] : a.n;   // neighbours are [j0, n)
     uint32_t *vb = reinterpret_cast<uint32_t *>(smem);
     size_t off = ((size_t)words * 4 + 15) & ~size_t(15);
     QEntry<HETERO> *q = reinterpret_cast<QEntry<HETERO> *>(smem + off) + warp * (kQueue + kQueue2);
@@ -346,14 +352,14 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
 
     int qn = 0, q2n = 0;
     constexpr int kStep = 32 * WPA;
-    int j = warp * 32 + lane;
+    int j = j0 + warp * 32 + lane;
     float xn = f.x, yn = f.y, rn = f.r;
     if (j < n) {
         xn = __ldg(a.x + j);
         yn = __ldg(a.y + j);
         if (HETERO) rn = __ldg(a.radius + j);
     }
-    for (int jb = warp * 32; jb < n; jb += kStep) {
+    for (int jb = j0 + warp * 32; jb < n; jb += kStep) {
         const float xj = xn, yj = yn, rj = rn;
         const bool valid = jb + lane < n;
         const int jn = jb + kStep + lane;   // prefetch the next chunk through L1
@@ -790,7 +796,9 @@ int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent) {
 static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
                        const abm_vf_params *p, const abm_agent_overrides *ov,
                        uint32_t *vpf_bits_dev, double *terms_dev, unsigned long long *diag_dev,
-                       cudaStream_t s, const GridDev *g, long long *sums, const char *fn) {
+                       cudaStream_t s, const GridDev *g, long long *sums, const char *fn,
+                       const int *seg_begin = nullptr, const int *seg_end = nullptr,
+                       const int *order = nullptr) {
     int st;
     int warps, tile, mode, wpa;
     abm_vpf_get_step_config(&warps, &tile);
@@ -819,10 +827,14 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     a.up = make_update(p);
     a.g = *g;
     a.sums = sums;
+    a.seg_begin = seg_begin;
+    a.seg_end = seg_end;
+    a.order = order;
     const bool torus = p->boundary == ABM_BOUNDARY_INFINITE;
     const bool hetero = a.radius != nullptr;
-    // auto: the l1 form while the positions fit comfortably in L1, tiled beyond
-    const bool use_l1 = mode == 1 || (mode == 0 && n <= 16384);
+    // auto: the l1 form while the positions fit comfortably in L1, tiled beyond; segmented
+    // (batched) swarms always use the l1 form
+    const bool use_l1 = seg_begin || mode == 1 || (mode == 0 && n <= 16384);
     if (use_l1) {
         if (!torus && !hetero) st = launch_l1<false, false>(a, wpa, s);
         else if (!torus && hetero) st = launch_l1<false, true>(a, wpa, s);
@@ -884,6 +896,26 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     long long *sums = (long long *)workspace(s, 32 * (size_t)n, &st);
     if (!sums) return st;
     return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, g, sums, fn);
+}
+
+int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32_t n_total,
+                          const int32_t *seg_begin_dev, const int32_t *seg_end_dev,
+                          const int32_t *order_dev, const abm_vf_params *p,
+                          const abm_agent_overrides *ov, uint32_t *vpf_bits_dev,
+                          double *terms_dev, unsigned long long *diag_dev, void *stream) {
+    const char *fn = "abm_vpf_flock_batched";
+    int st = step_validate(in, out, n_total, p, fn);
+    if (st || n_total == 0) return st;
+    if (!seg_begin_dev || !seg_end_dev)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: segment arrays are NULL", fn);
+    const GridDev *g = grid_for(p->rv, p->fov0, p->fov1, &st);
+    if (!g) return st;
+    if ((st = ensure_sincos_table())) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    long long *sums = (long long *)workspace(s, 32 * (size_t)n_total, &st);
+    if (!sums) return st;
+    return step_launch(in, out, n_total, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, g, sums,
+                       fn, seg_begin_dev, seg_end_dev, order_dev);
 }
 
 int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,

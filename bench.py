@@ -215,6 +215,104 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------- batched sweep leg
+BATCHED = dict(workload="vf_batched_sweep", n_instances=512, n_per_instance="uniform int [10,500]",
+               alp0_bet0="16 x 32 grid over [0.1, 3]", rv=1200, radius=10.0,
+               arena=[1000.0, 1000.0], boundary="walls", steps=2000, graph_chunk=100, seed=3)
+
+
+def batched_leg(torch, lib, stream, steps=BATCHED["steps"], flush=None):
+    """Batched sweep: 512 instances advanced by one abm_vpf_flock_batched call per step,
+    captured in CUDA graphs of 100 steps; compared with per-instance abm_vpf_flock_step calls
+    (eager, and captured as a graph of 512 x 2 launches per step)."""
+    import ctypes
+    from abm_gb300 import _lib
+    from abm_gb300.batched import BatchedSweep, sweep_instances
+    from abm_gb300.params import VFParams
+    vp = VFParams(gam=0.1, v0=1.0, alp1=0.08, bet1=0.08, width=1000.0, height=1000.0,
+                  rv=BATCHED["rv"], radius=BATCHED["radius"])
+    inst = sweep_instances(n_instances=BATCHED["n_instances"], seed=BATCHED["seed"])
+    b = BatchedSweep(vp, inst)
+    chunk = BATCHED["graph_chunk"]
+    b.capture(chunk)
+    b.run(chunk, chunk=chunk)                       # warm-up replay
+    torch.cuda.synchronize()
+    ev = []
+    done = 0
+    while done < steps:
+        if flush is not None:
+            flush.fill_(float(done))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.run(chunk, chunk=chunk)
+        e1.record()
+        ev.append((e0, e1))
+        done += chunk
+    torch.cuda.synchronize()
+    t_b = sum(a.elapsed_time(c) for a, c in ev) * 1e-3
+    agent_steps = b.n * done
+
+    # per-instance launches of the plain step (views into one concatenated state)
+    n_tot, offs = b.n, b.offsets
+    bufs = [{k: t.clone() for k, t in b._bufs[b._cur].items()},
+            {k: torch.empty_like(t) for k, t in b._bufs[b._cur].items()}]
+    cp = vp.to_c()
+    ov_t = b.ov_tensors
+
+    def per_instance_step(src, s):
+        for k in range(len(offs) - 1):
+            a0, a1 = int(offs[k]), int(offs[k + 1])
+            sl = lambda d: _lib.AbmSwarmState(*[_lib.fptr(d[key][a0:a1])
+                                                for key in ("x", "y", "theta", "v")])
+            ov = _lib.AbmAgentOverrides(None, _lib.fptr(ov_t["alp0"][a0:a1]),
+                                        _lib.fptr(ov_t["bet0"][a0:a1]), None)
+            si, so = sl(bufs[src]), sl(bufs[1 - src])
+            _lib.check(lib.abm_vpf_flock_step(ctypes.byref(si), ctypes.byref(so), a1 - a0,
+                                              ctypes.byref(cp), ctypes.byref(ov), None, None,
+                                              None, ctypes.c_void_p(s.cuda_stream)))
+
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        per_instance_step(0, s)                     # warm-up (workspace, tables)
+        s.synchronize()
+        k_eager = 10
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for k in range(k_eager):
+            per_instance_step(k % 2, s)
+        e1.record(s)
+        e1.synchronize()
+        t_eager = e0.elapsed_time(e1) * 1e-3 / k_eager
+        g = torch.cuda.CUDAGraph()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.graph(g, stream=s):
+            per_instance_step(0, s)
+            per_instance_step(1, s)
+        reps = 20
+        g.replay()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            g.replay()
+        e1.record(s)
+        e1.synchronize()
+        t_graph = e0.elapsed_time(e1) * 1e-3 / (2 * reps)
+    torch.cuda.current_stream().wait_stream(s)
+    per_step = t_b / done
+    return {"workload": dict(BATCHED, total_agents=n_tot,
+                             pairs_per_step=int((b.sizes.astype(np.int64) ** 2).sum()),
+                             l2="flushed between 100-step graph replays"),
+            "value": agent_steps / t_b, "unit": METRIC, "ms_per_step": per_step * 1e3,
+            "steps": done, "gpu_launches": 2 * done,
+            "per_instance_launches": {"eager_value": n_tot / t_eager,
+                                      "graph_value": n_tot / t_graph,
+                                      "ms_per_step_eager": t_eager * 1e3,
+                                      "ms_per_step_graph": t_graph * 1e3,
+                                      "launches_per_step": 2 * BATCHED["n_instances"]},
+            "speedup_vs_per_instance_graph": t_graph / per_step}
+
+
 # ---------------------------------------------------------------------- GPU arm
 def run_gb300(args, rank, world):
     import torch
@@ -328,6 +426,8 @@ def run_gb300(args, rank, world):
             "roofline": roofline, "clocks": clk,
             "wall_s_timed_region": t_wall,
             "diagnostics": diag}
+    if not args.no_batched:
+        line["batched"] = batched_leg(torch, lib, stream, flush=flush)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(state)
     print(json.dumps(line), flush=True)
@@ -340,6 +440,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))

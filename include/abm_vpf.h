@@ -144,6 +144,24 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
                        unsigned long long *diag_dev, void *stream);
 
 /*
+ * Batched sweep: one snapshot step of many independent swarms (instances) in one pair launch
+ * and one update launch.  The reference runs such sweeps as one simulation per generated .env
+ * file, sequentially or as separate processes (metarunner.py:168-254,
+ * HPC_run_all_exp_distribute.sh); here the instances' agents are concatenated in one SoA state
+ * of n_total agents and agent i sees exactly the agents [seg_begin[i], seg_end[i]) of its own
+ * instance (which contain i).  Per-instance ALP0 / BET0 / V0 / radius go in the per-agent
+ * override arrays.  order_dev (nullable): a permutation of [0, n_total) giving the order in which
+ * agents are scheduled (put the largest instances first for load balance).  All instances share
+ * p (Rv, arena, boundary, GAM, ALP1, BET1 ...).  Results per instance are bit-identical to
+ * abm_vpf_flock_step on that instance alone.  Always uses the L1 form of the pair kernel.
+ */
+int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32_t n_total,
+                          const int32_t *seg_begin_dev, const int32_t *seg_end_dev,
+                          const int32_t *order_dev, const abm_vf_params *p,
+                          const abm_agent_overrides *ov, uint32_t *vpf_bits_dev,
+                          double *terms_dev, unsigned long long *diag_dev, void *stream);
+
+/*
  * Allocation-free variant of abm_vpf_flock_step (no counterpart in the reference): the same
  * step, arguments, results and status codes, for callers that cannot call cudaMalloc, such as
  * code running inside another framework's memory pool, a host that has reserved all device

@@ -1,0 +1,87 @@
+"""GPU tests of the batched sweep (abm_vpf_flock_batched / abm_gb300.batched).
+
+Each instance of a batched step must be bit-identical to the plain step of that instance alone
+(same kernels, same decisions), including per-instance ALP0/BET0 and multi-step runs through a
+captured CUDA graph; small instances are also checked against the oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import gpu_available
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+
+
+def _instances(seed=4):
+    from abm_gb300.batched import sweep_instances
+    inst = sweep_instances(n_instances=7, n_min=10, n_max=300, alp_grid=(3, 3), seed=seed,
+                           width=600.0, height=600.0)
+    inst[0] = {k: (v[:1] if isinstance(v, np.ndarray) else v) for k, v in inst[0].items()}
+    rng = np.random.default_rng(seed)
+    for d in inst:
+        d["v"] = rng.uniform(0, 1, len(d["x"])).astype(np.float32)
+    return inst
+
+
+def test_batched_step_matches_single_instances():
+    from abm_gb300.batched import BatchedSweep
+    from abm_gb300.params import VFParams
+    from abm_gb300.swarm import VFSwarm
+    vp = VFParams(alp1=0.08, bet1=0.08, width=600.0, height=600.0, rv=1200)
+    inst = _instances()
+    b = BatchedSweep(vp, inst)
+    b.step(want_vpf=True, want_terms=True)
+    bv, bt = b.vpf_numpy(), b.terms.cpu().numpy()
+    for k, d in enumerate(inst):
+        a0, a1 = int(b.offsets[k]), int(b.offsets[k + 1])
+        n = a1 - a0
+        s = VFSwarm(vp, d["x"], d["y"], d["theta"], d["v"], alp0=np.full(n, d["alp0"]),
+                    bet0=np.full(n, d["bet0"]))
+        s.step(want_vpf=True, want_terms=True)
+        assert np.array_equal(s.vpf_numpy(), bv[a0:a1]), k
+        assert np.array_equal(s.terms.cpu().numpy(), bt[a0:a1]), k
+        st = s.state_numpy()
+        bs = b.instance_state(k)
+        for key in st:
+            assert np.array_equal(st[key], bs[key]), (k, key)
+
+
+def test_batched_small_instances_vs_oracle():
+    from abm_gb300.batched import BatchedSweep
+    from abm_gb300.params import VFParams
+    vp = VFParams(alp1=0.08, bet1=0.08, width=600.0, height=600.0, rv=1200)
+    inst = _instances(seed=9)[:4]
+    b = BatchedSweep(vp, inst)
+    b.step(want_vpf=True, want_terms=True)
+    bv, bt = b.vpf_numpy(), b.terms.cpu().numpy()
+    for k, d in enumerate(inst):
+        a0, a1 = int(b.offsets[k]), int(b.offsets[k + 1])
+        p = dict(vp.oracle_dict(), alp0=d["alp0"], bet0=d["bet0"])
+        st = {key: np.asarray(d[key], np.float64) for key in ("x", "y", "theta", "v")}
+        ref = oracle.vf_step(st, p, want_margins=True)
+        near = np.any(ref["margins"] < 1e-9, axis=1)
+        assert np.all((bv[a0:a1] == ref["vpf"]).all(axis=1) | near), k
+        scale = np.maximum(np.abs(ref["terms"]), 1e-6)
+        assert np.all(np.abs(bt[a0:a1] - ref["terms"]) / scale <= 1e-5), k
+
+
+def test_batched_graph_run_matches_eager_steps():
+    from abm_gb300.batched import BatchedSweep
+    from abm_gb300.params import VFParams
+    vp = VFParams(alp1=0.08, bet1=0.08, width=600.0, height=600.0, rv=1200)
+    inst = _instances(seed=11)
+    g = BatchedSweep(vp, inst)
+    e = BatchedSweep(vp, inst)
+    g.run(24, chunk=10)          # 2 graph replays + 4 single steps
+    for _ in range(24):
+        e.step()
+    sg, se = g.state_numpy(), e.state_numpy()
+    for key in sg:
+        assert np.array_equal(sg[key], se[key]), key
