@@ -43,9 +43,10 @@ WORKLOAD = dict(workload="vf_large_swarm", n_agents=4096, radius=5.0, arena=[500
 # agent: F = 36 (N-1) + 4 Rv + 20, M = 3 (N-1).
 F_PAIR, F_PX, F_UPD, M_PAIR = 36, 4, 20, 3
 L2_FLUSH_BYTES = 256 << 20
-# DRAM traffic of one vpf_flock_step launch of this workload, from the ncu capture summarised
-# in profiles/vpf_flock_step_n4096_rv3600.md (dram__bytes_read.sum + dram__bytes_write.sum).
-NCU_TRAFFIC_BYTES = None
+# DRAM traffic of one launch of the dominant kernel (the pair kernel) of this workload, from the
+# ncu capture summarised in profiles/vpf_pairs_l1_n4096_rv3600.md
+# (dram__bytes_read.sum + dram__bytes_write.sum).
+NCU_TRAFFIC_BYTES = 297728
 
 
 def make_workload(seed=WORKLOAD["seed"], n=WORKLOAD["n_agents"]):
