@@ -34,6 +34,7 @@ ABM_NOALLOC_MAX_AGENTS = 65536
 ABM_NOALLOC_MAX_RV = 8192
 ABM_DIAG_COUNT = 8
 DIAG_PAIRS_RESOLVED, DIAG_NEAR_BOUNDARY, DIAG_NONFINITE, DIAG_TIMEOUTS = 0, 1, 2, 3
+DIAG_CAPACITY = 4
 
 
 class AbmVfParams(ctypes.Structure):
@@ -80,6 +81,9 @@ SIGNATURES = [
     ("abm_vswrm_integrals", c_int32,
      [c_int32, c_int32, c_u32_p, c_double_p, c_float_p, c_double_p, c_float_p, c_float_p,
       c_float_p, c_double_p, c_void_p]),
+    ("abm_vpf_social_fields", c_int32,
+     [c_float_p, c_float_p, c_float_p, c_float_p, c_double, c_i32_p, c_i32_p, c_int32, c_double,
+      c_int32, c_int32, c_int32, c_double, c_double, c_u32_p, c_u64_p, c_void_p]),
     ("abm_vpf_set_step_config", c_int32, [c_int32, c_int32]),
     ("abm_vpf_get_step_config", c_int32, [c_i32_p, c_i32_p]),
     ("abm_vpf_set_step_mode", c_int32, [c_int32, c_int32]),

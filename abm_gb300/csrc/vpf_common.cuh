@@ -272,7 +272,7 @@ __device__ __forceinline__ void pair_offset(const FocalDev &f, float xj, float y
 // decisions that fall inside the guard bands.
 struct PairEst {
     int t, h;
-    float u, ps2;
+    float u, ps2, ca;
     bool unc_t, unc_h;
 };
 
@@ -332,6 +332,7 @@ __device__ __forceinline__ PairEst estimate_pair(const FocalDev &f, float dx, fl
     }
     r.u = u;
     r.ps2 = ps2;
+    r.ca = ca;
     return r;
 }
 

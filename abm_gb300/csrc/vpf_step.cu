@@ -331,7 +331,7 @@ static size_t l1_smem_bytes(int wpa, int words, bool hetero) {
 
 template <bool TORUS, bool HETERO, int WPA>
 __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int words = a.g.words;
     const int i = a.order ? a.order[blockIdx.x] : blockIdx.x;

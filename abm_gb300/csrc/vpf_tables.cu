@@ -258,6 +258,42 @@ const GridDev *grid_for_phi(int rv, const double *phi, int *status) {
     return &res.first->second.g;
 }
 
+// cos/sin(k 2pi / kSinCosTab) as double-float pairs in global memory (per device), for
+// kernels outside the translation unit that holds the __constant__ copy.
+const float4 *sincos_table_dev(int *status) {
+    static std::mutex mu;
+    static std::map<int, const float4 *> tabs;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = tabs.find(dev);
+    if (it != tabs.end()) {
+        *status = ABM_OK;
+        return it->second;
+    }
+    std::vector<float> tab(4 * (size_t)kSinCosTab);
+    for (int k = 0; k < kSinCosTab; ++k) {
+        const long double a = (long double)k * 2.0L * 3.14159265358979323846264338327950288L /
+                              (long double)kSinCosTab;
+        const long double c = cosl(a), sn = sinl(a);
+        const float ch = (float)c, sh = (float)sn;
+        tab[4 * k] = ch;
+        tab[4 * k + 1] = (float)(c - (long double)ch);
+        tab[4 * k + 2] = sh;
+        tab[4 * k + 3] = (float)(sn - (long double)sh);
+    }
+    void *mem = nullptr;
+    std::vector<void *> ptrs;
+    int st = upload({{tab.data(), tab.size() * sizeof(float)}}, &mem, ptrs);
+    if (st) {
+        *status = st;
+        return nullptr;
+    }
+    tabs[dev] = (const float4 *)ptrs[0];
+    *status = ABM_OK;
+    return (const float4 *)ptrs[0];
+}
+
 }  // namespace abm
 
 using namespace abm;

@@ -101,6 +101,8 @@ typedef struct abm_agent_overrides {
                                         of a pixel / width boundary (reported, not excused) */
 #define ABM_DIAG_NONFINITE 2         /* agents whose state was NaN / inf */
 #define ABM_DIAG_TIMEOUTS 3          /* bounded waits that gave up */
+#define ABM_DIAG_CAPACITY 4          /* social fields left empty: more obstacles in range than
+                                        the kernel's per-agent capacity (4096) */
 #define ABM_DIAG_COUNT 8
 
 /* ---------------------------------------------------------------- utilities */
@@ -210,6 +212,26 @@ int abm_vswrm_integrals(int32_t n_fields, int32_t rv, const uint32_t *bits_dev,
                         const double *phi_host, const float *vel_dev, const double prm[8],
                         const float *alp0_dev, const float *bet0_dev, const float *v0_dev,
                         double *out_dev, void *stream);
+
+/*
+ * Foraging social channel (Agent.calc_social_V_proj, abm/agent/agent.py:396-419, with
+ * Agent.projection_field :457-597 and exlude_V_source_data :421-445): for every agent i, the
+ * projection of the exploiting agents within vision_range (social cues: exploit[j] != 0,
+ * j != i, patch[j] != -1 and, when patchwise, patch[j] != patch[i]), where every other agent in
+ * range occludes them through the reference's distance-ordered interval trimming when
+ * visual_exclusion != 0.  Obstacle centres use the focal radius (agent.py:504-505); the range
+ * filter uses each agent's own radius (supcalc.py:73-78).  radius_dev may be NULL (all agents
+ * have `radius`).  out_bits_dev: n * abm_vpf_words(rv) uint32 in the reference's STORED order
+ * of soc_v_field (flipped, and zero where phis < fov0 or phis > fov1).  Requires
+ * -pi <= fov0 < fov1 <= pi; at most 4096 obstacles per agent (more: that field is left empty
+ * and ABM_DIAG_CAPACITY counts it).
+ */
+int abm_vpf_social_fields(const float *x_dev, const float *y_dev, const float *theta_dev,
+                          const float *radius_dev, double radius, const int32_t *exploit_dev,
+                          const int32_t *patch_dev, int32_t n, double vision_range,
+                          int32_t visual_exclusion, int32_t patchwise, int32_t rv, double fov0,
+                          double fov1, uint32_t *out_bits_dev, unsigned long long *diag_dev,
+                          void *stream);
 
 /* ---------------------------------------------------------------- launch configuration */
 
