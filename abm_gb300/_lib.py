@@ -51,6 +51,11 @@ class AbmSwarmState(ctypes.Structure):
     _fields_ = [("x", c_float_p), ("y", c_float_p), ("theta", c_float_p), ("v", c_float_p)]
 
 
+class AbmSwarmStateF64(ctypes.Structure):
+    _fields_ = [("x", c_double_p), ("y", c_double_p), ("theta", c_double_p),
+                ("v", c_double_p)]
+
+
 class AbmAgentOverrides(ctypes.Structure):
     _fields_ = [("radius", c_float_p), ("alp0", c_float_p), ("bet0", c_float_p),
                 ("v0", c_float_p)]
@@ -84,6 +89,20 @@ SIGNATURES = [
     ("abm_vpf_social_fields", c_int32,
      [c_float_p, c_float_p, c_float_p, c_float_p, c_double, c_i32_p, c_i32_p, c_int32, c_double,
       c_int32, c_int32, c_int32, c_double, c_double, c_u32_p, c_u64_p, c_void_p]),
+    ("abm_vpf_edge_fwd", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
+      ctypes.POINTER(AbmVfParams), c_int32, c_float_p, c_void_p]),
+    ("abm_vpf_edge_bwd", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState),
+      ctypes.POINTER(AbmSwarmState), c_double_p, c_int32, ctypes.POINTER(AbmVfParams), c_int32,
+      c_void_p]),
+    ("abm_vpf_edge_fwd_f64", c_int32,
+     [ctypes.POINTER(AbmSwarmStateF64), ctypes.POINTER(AbmSwarmStateF64), c_int32,
+      ctypes.POINTER(AbmVfParams), c_int32, c_double_p, c_void_p]),
+    ("abm_vpf_edge_bwd_f64", c_int32,
+     [ctypes.POINTER(AbmSwarmStateF64), ctypes.POINTER(AbmSwarmStateF64),
+      ctypes.POINTER(AbmSwarmStateF64), c_double_p, c_int32, ctypes.POINTER(AbmVfParams),
+      c_int32, c_void_p]),
     ("abm_vpf_set_step_config", c_int32, [c_int32, c_int32]),
     ("abm_vpf_get_step_config", c_int32, [c_i32_p, c_i32_p]),
     ("abm_vpf_set_step_mode", c_int32, [c_int32, c_int32]),

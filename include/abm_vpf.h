@@ -87,6 +87,11 @@ typedef struct abm_swarm_state {
     float *x, *y, *theta, *v;
 } abm_swarm_state;
 
+/* The same state in double precision (used by the FP64 mode of the edge form). */
+typedef struct abm_swarm_state_f64 {
+    double *x, *y, *theta, *v;
+} abm_swarm_state_f64;
+
 /* Optional per-agent device arrays (any may be NULL): radius (object_sizes / agent radius),
  * and the VFAgent.ALP0 / BET0 / V0 heterogeneity overrides (vf_agent.py:24-26). */
 typedef struct abm_agent_overrides {
@@ -232,6 +237,37 @@ int abm_vpf_social_fields(const float *x_dev, const float *y_dev, const float *t
                           int32_t visual_exclusion, int32_t patchwise, int32_t rv, double fov0,
                           double fov1, uint32_t *out_bits_dev, unsigned long long *diag_dev,
                           void *stream);
+
+/*
+ * Continuum edge form (differentiable; no counterpart in the reference, which only has the
+ * pixel form): neighbour j covers the retina arc [b_j - a_j, b_j + a_j] (b_j the closed angle
+ * of vf_supcalc.py:142-158, a_j = atan(R/d_j) like vf_supcalc.py:96-99, or asin(R/d_j) when
+ * use_asin != 0); with the merged arcs [l, u] of the union the VSWRM integrals are
+ * blob_c = -sum(sin u - sin l), blob_s = sum(cos u - cos l), edge_c = sum(cos l + cos u),
+ * edge_s = sum(sin l + sin u) (the Rv -> infinity limit of vf_supcalc.py:233-238), and the
+ * update is the reference's with increments scaled by p->dt (walls only).  Float32, n <= 2048.
+ * abm_vpf_edge_fwd: one step in -> out; terms_dev (nullable) n x 4 floats
+ *   {blob_c, blob_s, edge_c, edge_s}.
+ * abm_vpf_edge_bwd: the adjoint of that step: given grad_out = d loss / d out, OVERWRITES
+ *   grad_in with d loss / d in and ADDS d loss / d (alp0, alp1, bet0, bet1, v0) to the five
+ *   doubles of grad_params_dev.  The arc structure is recomputed from `in`.
+ * The _f64 variants run the same kernels in double precision.  The edge form is piecewise
+ * smooth: merges and splits of arcs are events where the edge terms jump, and over long
+ * horizons float32 rounding changes which events happen (a float32 rollout of 256 agents x 200
+ * steps at dt = 0.1 drifts by pixels from its FP64 twin), so gradients that must match an FP64
+ * reference over such horizons need the _f64 variants.
+ */
+int abm_vpf_edge_fwd(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
+                     const abm_vf_params *p, int32_t use_asin, float *terms_dev, void *stream);
+int abm_vpf_edge_bwd(const abm_swarm_state *in, const abm_swarm_state *grad_out,
+                     abm_swarm_state *grad_in, double *grad_params_dev, int32_t n,
+                     const abm_vf_params *p, int32_t use_asin, void *stream);
+int abm_vpf_edge_fwd_f64(const abm_swarm_state_f64 *in, abm_swarm_state_f64 *out, int32_t n,
+                         const abm_vf_params *p, int32_t use_asin, double *terms_dev,
+                         void *stream);
+int abm_vpf_edge_bwd_f64(const abm_swarm_state_f64 *in, const abm_swarm_state_f64 *grad_out,
+                         abm_swarm_state_f64 *grad_in, double *grad_params_dev, int32_t n,
+                         const abm_vf_params *p, int32_t use_asin, void *stream);
 
 /* ---------------------------------------------------------------- launch configuration */
 
