@@ -314,6 +314,73 @@ def batched_leg(torch, lib, stream, steps=BATCHED["steps"], flush=None):
             "speedup_vs_per_instance_graph": t_graph / per_step}
 
 
+# ---------------------------------------------------------------------- differentiable leg
+ADJOINT = dict(workload="vf_differentiable", n_agents=256, radius=10.0, arena=[1500.0, 1500.0],
+               steps=200, dt=0.1, checkpoint=20,
+               loss="1 - polarisation + MSE(mean position, seeded target)",
+               wrt="alp0, alp1, bet0, bet1, v0 and initial x, y, theta", seed=11)
+
+
+def adjoint_leg(torch):
+    """Edge-form rollout of the differentiable workload: forward only vs forward + adjoint
+    (gradients of the loss w.r.t. the five parameters and the initial state), best of 3 wall
+    times with the device synchronised, in the float32 and the FP64 kernels."""
+    import time as _t
+    from abm_gb300 import edge
+    from abm_gb300.params import VFParams
+    W = ADJOINT["arena"][0]
+    n, steps = ADJOINT["n_agents"], ADJOINT["steps"]
+    rng = np.random.default_rng(ADJOINT["seed"])
+    x0 = rng.uniform(30, 30 + W - 20, n)
+    y0 = rng.uniform(30, 30 + W - 20, n)
+    th0 = rng.uniform(0, 2 * np.pi, n)
+    base = VFParams(gam=0.1, v0=1.0, alp0=1.0, alp1=0.08, bet0=1.0, bet1=0.08, width=W,
+                    height=W, window_pad=30.0, radius=ADJOINT["radius"], dt=ADJOINT["dt"],
+                    rv=1200)
+    target = (0.45 * W, 0.55 * W)
+    out = {}
+    for name, dtype in (("fp32", torch.float32), ("fp64", torch.float64)):
+        def make(grad):
+            p = torch.tensor([1.0, 0.08, 1.0, 0.08, 1.0], dtype=torch.float64, device="cuda",
+                             requires_grad=grad)
+            init = [torch.tensor(a, dtype=dtype, device="cuda", requires_grad=grad)
+                    for a in (x0, y0, th0, np.zeros(n))]
+            return p, init
+
+        def fwd():
+            p, init = make(False)
+            with torch.no_grad():
+                edge.rollout(p, *init, base=base, steps=steps,
+                             checkpoint=ADJOINT["checkpoint"])
+
+        def fwd_bwd():
+            p, init = make(True)
+            o = edge.rollout(p, *init, base=base, steps=steps, checkpoint=ADJOINT["checkpoint"])
+            L = edge.flocking_loss(o[0], o[1], o[2],
+                                   torch.tensor(target, dtype=dtype, device="cuda"))
+            L.backward()
+
+        times = {}
+        for label, fn in (("fwd", fwd), ("fwd_adjoint", fwd_bwd)):
+            fn()
+            torch.cuda.synchronize()
+            best = float("inf")
+            for _ in range(3):
+                t0 = _t.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                best = min(best, _t.perf_counter() - t0)
+            times[label] = best
+        out[name] = {"fwd_agent_steps_per_s": n * steps / times["fwd"],
+                     "fwd_adjoint_agent_steps_per_s": n * steps / times["fwd_adjoint"],
+                     "fwd_ms": times["fwd"] * 1e3, "fwd_adjoint_ms": times["fwd_adjoint"] * 1e3,
+                     "cost_ratio_fwd_adjoint_over_fwd": times["fwd_adjoint"] / times["fwd"],
+                     "gpu_launches": {"fwd": steps,
+                                      "fwd_adjoint": 2 * steps + steps}}
+    return {"workload": ADJOINT, "unit": METRIC, **out,
+            "timing": "wall clock, device synchronised, best of 3 (includes host launch loop)"}
+
+
 # ---------------------------------------------------------------------- GPU arm
 def run_gb300(args, rank, world):
     import torch
@@ -429,6 +496,8 @@ def run_gb300(args, rank, world):
             "diagnostics": diag}
     if not args.no_batched:
         line["batched"] = batched_leg(torch, lib, stream, flush=flush)
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_leg(torch)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(state)
     print(json.dumps(line), flush=True)
@@ -442,6 +511,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))
