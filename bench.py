@@ -447,14 +447,11 @@ def run_gb300(args, rank, world):
     e2e_s = float(sum(a.elapsed_time(b) for a, b in ev2)) * 1e-3
     clk = clocks.stop()
 
-    if world > 1:
-        t = torch.tensor([kernel_s, e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        kernel_s, e2e_s = float(t[0]), float(t[1])
+    from abm_gb300.replicas import combine
+    (kernel_s, e2e_s), agent_steps = combine([kernel_s, e2e_s], n * args.steps, device=dev)
     if rank != 0:
         return
 
-    agent_steps = n * args.steps * world
     value = agent_steps / kernel_s
     e2e_value = agent_steps / e2e_s
     t_launch = kernel_s / args.steps

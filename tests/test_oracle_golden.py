@@ -33,10 +33,8 @@ def test_known_answer_closed_angle():
         assert oracle.calculate_closed_angle(v1, v2) == exp
 
 
-@pytest.mark.parametrize("rv", list(range(8, 5001)))
+@pytest.mark.parametrize("rv", sorted(set(range(8, 5001, 97)) | {61, 122, 197, 1200, 2666, 3600}))
 def test_arange_and_linspace_match_numpy(rv):
-    if rv % 97 and rv not in (61, 122, 197, 1200, 3600, 2666):
-        pytest.skip("sampled")
     assert np.array_equal(oracle.arange_phi(rv), np.arange(-np.pi, np.pi, 2 * np.pi / rv))
     assert np.array_equal(oracle.linspace(rv), np.linspace(-np.pi, np.pi, rv))
 
