@@ -91,6 +91,12 @@ __device__ __forceinline__ float atan_poly(float s) {
     return p;
 }
 
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
@@ -258,8 +264,9 @@ template <bool TORUS, bool HETERO>
 __device__ __forceinline__ void pair_offset(const FocalDev &f, float xj, float yj, float rj,
                                             dfl W, dfl H, float &dx, float &dy) {
     if (!TORUS && !HETERO) {
-        dx = xj - f.x;
-        dy = yj - f.y;
+        const float2 d = __fadd2_rn(make_float2(xj, yj), make_float2(-f.x, -f.y));
+        dx = d.x;
+        dy = d.y;
     } else {
         dfl ex, ey;
         exact_offset<TORUS, HETERO>(f, xj, yj, rj, W, H, ex, ey);
@@ -295,8 +302,10 @@ template <bool HETERO>
 __device__ __forceinline__ PairEst estimate_pair(const FocalDev &f, float dx, float dy, float rj,
                                                  float invrj, const GridDev &g) {
     PairEst r;
-    const float d2 = fmaf(dx, dx, dy * dy);
-    const float rsq = rsqrtf(d2);
+    // d^2 >= 1e-30 keeps rsqrt finite for offsets below 1e-15 px (flush-to-zero range)
+    const float d2raw = fmaf(dx, dx, dy * dy);
+    const float d2 = fmaxf(d2raw, 1e-30f);
+    const float rsq = rsqrt_approx(d2);
     // (P, Q) = (c dy + s dx, c dx - s dy): cross and dot of the heading with the offset
     const float2 PQ = __ffma2_rn(make_float2(f.c, f.c), make_float2(dy, dx),
                                  __fmul2_rn(make_float2(f.s, -f.s), make_float2(dx, dy)));
@@ -325,7 +334,7 @@ __device__ __forceinline__ PairEst estimate_pair(const FocalDev &f, float dx, fl
     r.h = (int)hf;
     r.unc_t = fabsf(fr.x) < g.band_t || fabsf(u - g.half_rm1) > g.half_rm1 - g.band_t;
     r.unc_h = fabsf(fr.y) > 0.5f - g.band_h * fmaxf(ps2, 1.f);
-    if (HETERO && d2 == 0.f) {  // coincident centres: atan(R/0) = pi/2, NaN bearing -> pixel 0
+    if (HETERO && d2raw == 0.f) {  // coincident centres: atan(R/0) = pi/2, NaN bearing -> px 0
         r.t = 0;
         r.h = g.rv >> 2;
         r.unc_t = r.unc_h = false;
@@ -338,7 +347,9 @@ __device__ __forceinline__ PairEst estimate_pair(const FocalDev &f, float dx, fl
 
 // Visibility test of vf_supcalc.py:119 (strict, on the pixel indices).
 __device__ __forceinline__ bool projection_visible(const GridDev &g, int s, int e) {
-    return (g.f0 < s && s < g.f1) || (g.f0 < e && e < g.f1);
+    // f0 < k < f1  <=>  (unsigned)(k - f0 - 1) < (unsigned)(f1 - f0 - 1)
+    const unsigned span = (unsigned)(g.f1 - g.f0 - 1);
+    return (unsigned)(s - g.f0 - 1) < span || (unsigned)(e - g.f0 - 1) < span;
 }
 
 // OR a visible projection [s, e) into the bitmask; the common case (no wrap, at most 32
@@ -414,69 +425,6 @@ __device__ __forceinline__ void warp_integrals(const uint32_t *vb, const GridDev
     }
 }
 
-// ------------------------------------------------------------------ agent update (FP64)
-struct UpdateParams {
-    double gam, v0, alp0, alp1, bet0, bet1;
-    double max_vel, max_th, dt;
-    double bx0, bx1, by0, by1;
-    int limit, torus;
-};
-
-__device__ __forceinline__ double prove_orientation(double th) {  // agent.py:605-610
-    if (th < 0) th = 2 * kPi + th;
-    if (th > kPi * 2) th = th - 2 * kPi;
-    return th;
-}
-
-// VFAgent.update_agent_position (vf_agent.py:289-309), prove_turning/prove_velocity
-// (:311-327), then Agent.reflect_from_walls (agent.py:347-394) or
-// VFAgent.teleport_infinite_arena (vf_agent.py:188-204).
-__device__ __forceinline__ void update_agent(const UpdateParams &p, double R, double dpsi,
-                                             double dv, double &x, double &y, double &th,
-                                             double &v) {
-    double theta = dpsi * p.dt;
-    if (p.limit && fabs(theta) > p.max_th) theta = p.max_th * (theta < 0 ? -1.0 : 1.0);
-    th = prove_orientation(th + theta);
-    v += dv * p.dt;
-    if (p.limit && fabs(v) > p.max_vel) v = p.max_vel * (v < 0 ? -1.0 : 1.0);
-    double sn, cs;
-    sincos(th, &sn, &cs);
-    x = x + (v * p.dt) * cs;
-    y = y - (v * p.dt) * sn;
-    const double cx = x + R, cy = y + R;
-    if (!p.torus) {
-        if (cx < p.bx0) {
-            x = p.bx0 - R;
-            if (kPi / 2 <= th && th < kPi) th -= kPi / 2;
-            else if (kPi <= th && th <= 3 * kPi / 2) th += kPi / 2;
-            th = prove_orientation(th);
-        }
-        if (cx > p.bx1) {
-            x = p.bx1 - R - 1;
-            if (3 * kPi / 2 <= th && th < 2 * kPi) th -= kPi / 2;
-            else if (0 <= th && th <= kPi / 2) th += kPi / 2;
-            th = prove_orientation(th);
-        }
-        if (cy < p.by0) {
-            y = p.by0 - R;
-            if (kPi / 2 <= th && th <= kPi) th += kPi / 2;
-            else if (0 <= th && th < kPi / 2) th -= kPi / 2;
-            th = prove_orientation(th);
-        }
-        if (cy > p.by1) {
-            y = p.by1 - R - 1;
-            if (3 * kPi / 2 <= th && th <= 2 * kPi) th += kPi / 2;
-            else if (kPi <= th && th < 3 * kPi / 2) th -= kPi / 2;
-            th = prove_orientation(th);
-        }
-    } else {
-        if (cx < p.bx0) x = p.bx1 - R;
-        else if (cx > p.bx1) x = p.bx0 + R;
-        if (cy < p.by0) y = p.by1 - R;
-        else if (cy > p.by1) y = p.by0 + R;
-    }
-}
-
 // ------------------------------------------------------------------ double-float sincos
 // cos/sin of a float32 angle to ~1e-14 using FP32 arithmetic only (GB300's FP64 pipe is
 // ~1/64 of its FP32 rate, and a lane-masked FP64 instruction costs a full warp's time):
@@ -503,6 +451,138 @@ __device__ __forceinline__ void df_sincos(float theta, const float4 *tab, dfl &c
     const dfl ck = {t.x, t.y}, sk = {t.z, t.w};
     c = df_sub(df_mul(ck, cr), df_mul(sk, sr));
     s = df_add(df_mul(sk, cr), df_mul(ck, sr));
+}
+
+// cos/sin of a double-float angle (same method; the low part joins the reduced argument).
+__device__ __forceinline__ void df_sincos_df(dfl theta, const float4 *tab, dfl &c, dfl &s) {
+    const float inv_h = 1.629746552e+02f;
+    const dfl H = {6.135923322e-03f, -1.707476105e-10f};
+    const float kf = rintf(theta.hi * inv_h);
+    int k = (int)kf;
+    dfl r = df_sub(theta, df_add(two_prod(kf, H.hi), two_prod(kf, H.lo)));
+    k &= (kSinCosTab - 1);
+    const dfl r2 = df_mul(r, r);
+    const dfl sixth = {1.666666716e-01f, -4.967053879e-09f};
+    const dfl s_in = df_sub(sixth, df_mul(r2, dfl{8.333333768e-03f, -4.346172033e-10f}));
+    const dfl sr = df_mul(r, df_sub(dfl{1.f, 0.f}, df_mul(r2, s_in)));
+    const dfl c_in = df_sub(dfl{0.5f, 0.f}, df_mul(r2, dfl{4.166666791e-02f, -1.241763470e-09f}));
+    const dfl cr = df_sub(dfl{1.f, 0.f}, df_mul(r2, c_in));
+    const float4 t = tab[k];
+    const dfl ck = {t.x, t.y}, sk = {t.z, t.w};
+    c = df_sub(df_mul(ck, cr), df_mul(sk, sr));
+    s = df_add(df_mul(sk, cr), df_mul(ck, sr));
+}
+
+// ------------------------------------------------------------------ agent update (double-float)
+// The reference's update (vf_agent.py:289-327, agent.py:347-394 / vf_agent.py:188-204) in
+// double-float arithmetic on the FP32 pipe, so it can run in the pair kernel's epilogue (one
+// lane per agent) without FP64 instructions.  Results are rounded to float32 once at the end.
+struct UpdateDf {
+    dfl gam, v0, alp0, alp1, bet0, bet1;   // parameters (per-agent overrides replace alp0...)
+    dfl max_vel, max_th, dt;
+    dfl bx0, bx1, by0, by1;
+    int limit, torus, phi_ok;
+};
+
+__device__ __forceinline__ dfl df_from_fix(long long v) {   // v * 2^-40 in double-float
+    const float hi = (float)v;
+    const float lo = (float)(v - (long long)hi);
+    return fast_two_sum(hi * 9.094947017729282e-13f, lo * 9.094947017729282e-13f);
+}
+
+__device__ __forceinline__ dfl df_prove_orientation(dfl t) {   // agent.py:605-610
+    const dfl two_pi = {6.283185482e+00f, -1.748455531e-07f};
+    if (df_sign(t) < 0) t = df_add(two_pi, t);
+    if (df_sign(df_sub(t, two_pi)) > 0) t = df_sub(t, two_pi);
+    return t;
+}
+
+__device__ __forceinline__ bool df_lt(dfl a, dfl b) { return df_sign(df_sub(a, b)) < 0; }
+__device__ __forceinline__ bool df_le(dfl a, dfl b) { return df_sign(df_sub(a, b)) <= 0; }
+
+struct UpdateOut {
+    float x, y, th, v;
+    dfl terms[6];   // dvel, dpsi, alpha_blob, alpha_edge, beta_blob, beta_edge
+};
+
+static __device__ __noinline__ UpdateOut update_agent_df(const UpdateDf &p, const float4 *sctab,
+                                                  float xf, float yf, float thf, float vf,
+                                                  float Rf, long long bc, long long bs,
+                                                  long long ec, long long es, dfl alp0,
+                                                  dfl bet0, dfl v0) {
+    const dfl half_pi = {1.570796371e+00f, -4.371138829e-08f};
+    const dfl pi = {3.141592741e+00f, -8.742277657e-08f};
+    const dfl three_half_pi = {4.712388992e+00f, -1.192488064e-08f};
+    const dfl two_pi = {6.283185482e+00f, -1.748455531e-07f};
+    const dfl zero = {0.f, 0.f};
+    UpdateOut o;
+    dfl ab = zero, ae = zero, bb = zero, be = zero, dv = zero, dpsi = zero;
+    const dfl vel = {vf, 0.f};
+    if (p.phi_ok) {
+        ab = df_mul(alp0, df_neg(df_from_fix(bc)));
+        ae = df_mul(df_mul(alp0, p.alp1), df_from_fix(ec));
+        bb = df_mul(bet0, df_neg(df_from_fix(bs)));
+        be = df_mul(df_mul(bet0, p.bet1), df_from_fix(es));
+        dv = df_add(df_add(df_mul(p.gam, df_sub(v0, vel)), ab), ae);
+        dpsi = df_add(bb, be);
+    }
+    o.terms[0] = dv;
+    o.terms[1] = dpsi;
+    o.terms[2] = ab;
+    o.terms[3] = ae;
+    o.terms[4] = bb;
+    o.terms[5] = be;
+    dfl theta = df_mul(dpsi, p.dt);
+    if (p.limit && df_lt(p.max_th, dfl{fabsf(theta.hi), theta.hi < 0 ? -theta.lo : theta.lo}))
+        theta = (df_sign(theta) < 0) ? df_neg(p.max_th) : p.max_th;
+    dfl th = df_prove_orientation(df_add(dfl{thf, 0.f}, theta));
+    dfl v = df_add(vel, df_mul(dv, p.dt));
+    if (p.limit && df_lt(p.max_vel, dfl{fabsf(v.hi), v.hi < 0 ? -v.lo : v.lo}))
+        v = (df_sign(v) < 0) ? df_neg(p.max_vel) : p.max_vel;
+    dfl cs, sn;
+    df_sincos_df(th, sctab, cs, sn);
+    const dfl vdt = df_mul(v, p.dt);
+    dfl x = df_add(dfl{xf, 0.f}, df_mul(vdt, cs));
+    dfl y = df_sub(dfl{yf, 0.f}, df_mul(vdt, sn));
+    const dfl R = {Rf, 0.f};
+    const dfl cx = df_add(x, R), cy = df_add(y, R);
+    const dfl one = {1.f, 0.f};
+    if (!p.torus) {
+        if (df_lt(cx, p.bx0)) {
+            x = df_sub(p.bx0, R);
+            if (df_le(half_pi, th) && df_lt(th, pi)) th = df_sub(th, half_pi);
+            else if (df_le(pi, th) && df_le(th, three_half_pi)) th = df_add(th, half_pi);
+            th = df_prove_orientation(th);
+        }
+        if (df_lt(p.bx1, cx)) {
+            x = df_sub(df_sub(p.bx1, R), one);
+            if (df_le(three_half_pi, th) && df_lt(th, two_pi)) th = df_sub(th, half_pi);
+            else if (df_le(zero, th) && df_le(th, half_pi)) th = df_add(th, half_pi);
+            th = df_prove_orientation(th);
+        }
+        if (df_lt(cy, p.by0)) {
+            y = df_sub(p.by0, R);
+            if (df_le(half_pi, th) && df_le(th, pi)) th = df_add(th, half_pi);
+            else if (df_le(zero, th) && df_lt(th, half_pi)) th = df_sub(th, half_pi);
+            th = df_prove_orientation(th);
+        }
+        if (df_lt(p.by1, cy)) {
+            y = df_sub(df_sub(p.by1, R), one);
+            if (df_le(three_half_pi, th) && df_le(th, two_pi)) th = df_add(th, half_pi);
+            else if (df_le(pi, th) && df_lt(th, three_half_pi)) th = df_sub(th, half_pi);
+            th = df_prove_orientation(th);
+        }
+    } else {
+        if (df_lt(cx, p.bx0)) x = df_sub(p.bx1, R);
+        else if (df_lt(p.bx1, cx)) x = df_add(p.bx0, R);
+        if (df_lt(cy, p.by0)) y = df_sub(p.by1, R);
+        else if (df_lt(p.by1, cy)) y = df_add(p.by0, R);
+    }
+    o.x = x.hi + x.lo;
+    o.y = y.hi + y.lo;
+    o.th = th.hi + th.lo;
+    o.v = v.hi + v.lo;
+    return o;
 }
 
 // ------------------------------------------------------------------ TMA bulk staging

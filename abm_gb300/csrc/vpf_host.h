@@ -26,8 +26,10 @@ const GridDev *grid_for(int rv, double fov0, double fov1, int *status);
 const GridDev *grid_for_phi(int rv, const double *phi, int *status);
 
 int np_arange_phi(int rv, std::vector<double> *out);
-// Per-device global copy of the double-float sincos table used by df_sincos.
+// Per-device global copy of the double-float sincos table used by df_sincos, and its host
+// construction (cos/sin(k 2 pi / kSinCosTab) as (cos hi, cos lo, sin hi, sin lo)).
 const float4 *sincos_table_dev(int *status);
+void sincos_table_host(std::vector<float> &tab);
 void np_linspace_pi(int n, std::vector<double> &out);
 int find_nearest(const std::vector<double> &a, double v);
 

@@ -1,17 +1,17 @@
 // vpf_step.cu -- the per-timestep hot path (VPF rasterisation + VSWRM integrals + agent update)
 // and the drop-in twins of projection_field / VSWRM_flocking_state_variables.
 //
-// One step is two launches:
-//  * a pair kernel: one warp per focal agent evaluates every neighbour (FP32 with a guard band
-//    and a double-float re-decision inside it), OR-s the visible pixel runs into the agent's
-//    VPF bitmask in shared memory and reduces the bitmask's transitions to the four VSWRM sums
-//    (fixed point).  Two forms: `l1` (single-warp blocks, neighbours read through the
-//    read-only L1 path; balanced to ~27 agents per SM, no block barriers) and `tiled`
-//    (several focal warps per block share neighbour tiles staged in shared memory by the TMA
-//    bulk engine, double-buffered with mbarriers; for swarms whose positions do not fit L1);
-//  * an update kernel: one thread per agent applies the FP64 VSWRM combination and the
-//    reference's heading / speed / position update and boundary rule, with all 32 lanes of
-//    every warp busy (a lane-masked FP64 instruction costs a whole warp's FP64 time on GB300).
+// One step is two launches.  The pair kernel runs one warp per focal agent: it evaluates every
+// neighbour (FP32 with a guard band and a double-float re-decision inside it), OR-s the visible
+// pixel runs into the agent's VPF bitmask in shared memory and reduces the bitmask's
+// transitions to the four VSWRM sums (fixed point).  The update kernel then applies the
+// reference's heading / speed / position update and boundary rule, one thread per agent, in
+// double-float arithmetic on the FP32 pipe (GB300's FP64 rate is a small fraction of its FP32
+// rate).  Two forms of the pair kernel:
+//  * `l1`: single-warp blocks, neighbours read through the read-only L1 path; about 27 agents
+//    per SM and no block barriers;
+//  * `tiled`: several focal warps per block share neighbour tiles staged in shared memory by the
+//    TMA bulk engine (double-buffered with mbarriers), for swarms whose positions exceed L1.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -33,8 +33,9 @@ struct StepArgs {
     double *terms;
     unsigned long long *diag;
     dfl W, H;
-    UpdateParams up;
     GridDev g;
+    UpdateDf ud;           // the update's parameters in double-float
+    const float4 *sctab;   // global copy of the double-float sincos table
     long long *sums;       // n x 4 workspace: bc, bs, ec, es of every agent
     // batched sweeps: agent i sees the agents [seg_begin[i], seg_end[i]) of its instance;
     // block b works on agent order[b] (largest instances first); all NULL for one swarm
@@ -70,27 +71,27 @@ static int ensure_sincos_table() {
     return st;
 }
 
-// Per-(device, stream) workspace for the per-agent sums (grown on demand, never shrunk).
-static void *workspace(cudaStream_t stream, size_t bytes, int *status) {
+// Per-(device, stream) workspace for the per-agent sums handed from the pair kernel to the
+// update kernel (32 B per agent).  A workspace that grows is replaced but the old one stays
+// allocated, since a CUDA graph captured from the stream may still use it.
+static long long *workspace(cudaStream_t stream, int n, int *status) {
     static std::mutex mu;
-    static std::map<std::pair<int, void *>, std::pair<void *, size_t>> ws;
+    static std::map<std::pair<int, void *>, std::pair<void *, long>> ws;
+    static std::vector<void *> retired;
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
     auto &e = ws[{dev, (void *)stream}];
-    if (e.second < bytes) {
-        if (e.first) {
-            cudaStreamSynchronize(stream);
-            cudaFree(e.first);
-        }
-        e = {nullptr, 0};
+    if (e.second < n) {
+        const long cap = std::max<long>(n, 1024);
         void *p = nullptr;
-        *status = check_cuda(cudaMalloc(&p, bytes), "cudaMalloc(step workspace)");
+        *status = check_cuda(cudaMalloc(&p, (size_t)cap * 32), "cudaMalloc(step workspace)");
         if (*status) return nullptr;
-        e = {p, bytes};
+        if (e.first) retired.push_back(e.first);
+        e = {p, cap};
     }
     *status = ABM_OK;
-    return e.first;
+    return (long long *)e.first;
 }
 
 // Per-warp work queues of the step kernel: candidate neighbours that survived the cull (their
@@ -123,16 +124,17 @@ struct QEntry<true> {
 };
 
 // ---------------------------------------------------------------------------- no-alloc scratch
-// Scratch of abm_vpf_flock_step_noalloc, for callers that cannot allocate device memory:
-// the per-agent sums (32 B x kNoAllocMaxAgents) and one grid's lookup tables (Rv up to
-// kNoAllocMaxRv), carved out of one file-scope array that every GPU loading the library holds
-// until the process exits (about 2.5 MiB).
+// Scratch of abm_vpf_flock_step_noalloc, for callers that cannot allocate device memory: the
+// per-agent sums (up to kNoAllocMaxAgents agents), one grid's lookup tables (Rv up to
+// kNoAllocMaxRv) and the double-float sincos table, carved out of one file-scope array that
+// every GPU loading the library holds until the process exits (about 2.5 MiB).
 constexpr int kNoAllocMaxAgents = 65536;
 constexpr int kNoAllocMaxRv = 8192;
 constexpr size_t kNaAlign = 256;
 constexpr size_t na_round(size_t b) { return (b + kNaAlign - 1) & ~(kNaAlign - 1); }
 constexpr size_t kNaSums = 0;
-constexpr size_t kNaMid = kNaSums + na_round(32ull * kNoAllocMaxAgents);
+constexpr size_t kNaSin = kNaSums + na_round(32ull * kNoAllocMaxAgents);
+constexpr size_t kNaMid = kNaSin + na_round(sizeof(float4) * kSinCosTab);
 constexpr size_t kNaCot2 = kNaMid + na_round(sizeof(float4) * kNoAllocMaxRv);
 constexpr size_t kNaQ = kNaCot2 + na_round(sizeof(float2) * (kNoAllocMaxRv / 4 + 2));
 constexpr size_t kNaCpt = kNaQ + na_round(sizeof(longlong2) * (kNoAllocMaxRv + 1));
@@ -142,6 +144,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
 struct NoAllocDevice {
     unsigned char *base = nullptr;   // device address of g_noalloc_scratch on this device
+    bool sincos_loaded = false;
     bool grid_loaded = false;        // which grid's tables the array holds
     int rv = 0;
     double fov0 = 0, fov1 = 0;
@@ -173,14 +176,14 @@ static NoAllocDevice *noalloc_device(int *status) {
 }
 
 // Heavy decision + rasterisation of up to 32 queued candidates (lane < cnt holds one).
-template <bool TORUS, bool HETERO>
+template <bool TORUS, bool HETERO, bool FULL = false>
 __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEntry<HETERO> *q,
                                                    int cnt, QEntry<HETERO> *q2, int &q2n,
                                                    uint32_t *vb, const StepArgs &a,
                                                    unsigned *cnt_resolved, unsigned *cnt_near) {
     const int lane = threadIdx.x & 31;
-    const bool have = lane < cnt;
-    QEntry<HETERO> e = have ? q[lane] : QEntry<HETERO>::make(f.x, f.y, f.r);
+    const bool have = FULL || lane < cnt;   // FULL: a batch of 32, every lane has a candidate
+    QEntry<HETERO> e = (FULL || have) ? q[lane] : QEntry<HETERO>::make(f.x, f.y, f.r);
     const float xj = e.x(), yj = e.y(), rj = e.r(a.radius0);
     float dx, dy;
     pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
@@ -291,24 +294,25 @@ __device__ __forceinline__ void enqueue_candidate(const FocalDev &f, bool live, 
     __syncwarp();
     if (qn >= 32) {   // warp-uniform
         qn -= 32;
-        process_candidates<TORUS, HETERO>(f, q + qn, 32, q2, q2n, vb, a, &counters[0],
+        process_candidates<TORUS, HETERO, true>(f, q + qn, 32, q2, q2n, vb, a, &counters[0],
                                           &counters[1]);
     }
 }
 
-// Warp epilogue of a focal agent: the integral sums and (optionally) the bitmask to global.
-__device__ __forceinline__ void store_agent(const StepArgs &a, int i, const uint32_t *vb) {
+// Warp epilogue of a focal agent: VSWRM integrals, the optional bitmask output and (lane 0)
+// the sums for the update kernel.
+__device__ __forceinline__ void finish_agent(const StepArgs &a, int i, const uint32_t *vb) {
     const int lane = threadIdx.x & 31;
     long long bc, bs, ec, es;
     warp_integrals(vb, a.g, bc, bs, ec, es);
-    if (lane == 0) {
-        longlong2 *dst = reinterpret_cast<longlong2 *>(a.sums + 4 * (size_t)i);
-        dst[0] = make_longlong2(bc, bs);
-        dst[1] = make_longlong2(ec, es);
-    }
     if (a.bits) {
         uint32_t *dst = a.bits + (size_t)i * a.g.words;
         for (int w = lane; w < a.g.words; w += 32) dst[w] = vb[w];
+    }
+    if (lane == 0) {
+        longlong2 *sp = reinterpret_cast<longlong2 *>(a.sums) + 2 * (size_t)i;
+        sp[0] = make_longlong2(bc, bs);
+        sp[1] = make_longlong2(ec, es);
     }
 }
 
@@ -376,7 +380,7 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
     drain_deferred<TORUS, HETERO>(f, q2, q2n, vb, a, &counters[0], &counters[1]);
     if (WPA > 1) __syncthreads(); else __syncwarp();
     if (warp == 0) {
-        store_agent(a, i, vb);
+        finish_agent(a, i, vb);
         if (lane == 0) flush_counters(a, counters);
     }
 }
@@ -493,10 +497,36 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
                                                       &counters[1]);
         drain_deferred<TORUS, HETERO>(f, q2, q2n, vb, a, &counters[0], &counters[1]);
         __syncwarp();
-        store_agent(a, i, vb);
+        finish_agent(a, i, vb);
     }
     __syncthreads();
     if (tid == 0) flush_counters(a, counters);
+}
+
+// ---------------------------------------------------------------------------- update kernel
+// The reference's update of every agent from its sums, one thread per agent.
+template <bool HETERO>
+__global__ void __launch_bounds__(64) vpf_update_kernel(const StepArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const longlong2 *sp = reinterpret_cast<const longlong2 *>(a.sums) + 2 * (size_t)k;
+    const longlong2 s0 = sp[0], s1 = sp[1];
+    const dfl alp0 = a.alp0 ? dfl{a.alp0[k], 0.f} : a.ud.alp0;
+    const dfl bet0 = a.bet0 ? dfl{a.bet0[k], 0.f} : a.ud.bet0;
+    const dfl v0 = a.v0 ? dfl{a.v0[k], 0.f} : a.ud.v0;
+    const float R = HETERO ? a.radius[k] : a.radius0;
+    const UpdateOut o = update_agent_df(a.ud, a.sctab, a.x[k], a.y[k], a.th[k], a.v[k], R,
+                                        s0.x, s0.y, s1.x, s1.y, alp0, bet0, v0);
+    a.xo[k] = o.x;
+    a.yo[k] = o.y;
+    a.tho[k] = o.th;
+    a.vo[k] = o.v;
+    if (a.terms) {
+        double *t = a.terms + 6 * (size_t)k;
+        for (int m = 0; m < 6; ++m) t[m] = (double)o.terms[m].hi + (double)o.terms[m].lo;
+    }
+    if (a.diag && !(isfinite(o.x) && isfinite(o.y) && isfinite(o.th) && isfinite(o.v)))
+        atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
 }
 
 // Evaluates the in-kernel double-float cos/sin (verification hook for the tests).
@@ -507,47 +537,6 @@ __global__ void check_sincos_kernel(const float *theta, int n, double *out) {
     df_sincos(theta[k], c_sincos, c, s);
     out[2 * k] = (double)c.hi + (double)c.lo;
     out[2 * k + 1] = (double)s.hi + (double)s.lo;
-}
-
-// ---------------------------------------------------------------------------- update
-// One thread per agent: VSWRM combination (vf_supcalc.py:233-254) and the state update.
-__global__ void __launch_bounds__(128) vpf_update_kernel(const StepArgs a) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n) return;
-    const UpdateParams &p = a.up;
-    const longlong2 s0 = reinterpret_cast<const longlong2 *>(a.sums)[2 * (size_t)k];
-    const longlong2 s1 = reinterpret_cast<const longlong2 *>(a.sums)[2 * (size_t)k + 1];
-    const double alp0 = a.alp0 ? (double)a.alp0[k] : p.alp0;
-    const double bet0 = a.bet0 ? (double)a.bet0[k] : p.bet0;
-    const double v0 = a.v0 ? (double)a.v0[k] : p.v0;
-    const double R = a.radius ? (double)a.radius[k] : (double)a.radius0;
-    double vel = (double)a.v[k];
-    double ab = 0, ae = 0, bb = 0, be = 0, dv = 0, dpsi = 0;
-    if (a.g.phi_ok) {
-        ab = alp0 * (-(double)s0.x * kInvFix);
-        ae = alp0 * p.alp1 * ((double)s1.x * kInvFix);
-        bb = bet0 * (-(double)s0.y * kInvFix);
-        be = bet0 * p.bet1 * ((double)s1.y * kInvFix);
-        dv = p.gam * (v0 - vel) + ab + ae;
-        dpsi = bb + be;
-    }
-    if (a.terms) {
-        double *t = a.terms + 6 * (size_t)k;
-        t[0] = dv;
-        t[1] = dpsi;
-        t[2] = ab;
-        t[3] = ae;
-        t[4] = bb;
-        t[5] = be;
-    }
-    double x = (double)a.x[k], y = (double)a.y[k], th = (double)a.th[k];
-    update_agent(p, R, dpsi, dv, x, y, th, vel);
-    a.xo[k] = (float)x;
-    a.yo[k] = (float)y;
-    a.tho[k] = (float)th;
-    a.vo[k] = (float)vel;
-    if (a.diag && !(isfinite(x) && isfinite(y) && isfinite(th) && isfinite(vel)))
-        atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
 }
 
 template <bool TORUS, bool HETERO>
@@ -576,23 +565,26 @@ static int launch_tiled(const StepArgs &a, int warps, cudaStream_t stream) {
 
 static bool aligned16(const void *p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; }
 
-UpdateParams make_update(const abm_vf_params *p) {
-    UpdateParams u;
-    u.gam = p->gam;
-    u.v0 = p->v0;
-    u.alp0 = p->alp0;
-    u.alp1 = p->alp1;
-    u.bet0 = p->bet0;
-    u.bet1 = p->bet1;
-    u.max_vel = p->max_vel;
-    u.max_th = p->max_th;
-    u.dt = p->dt;
-    u.bx0 = p->window_pad;
-    u.bx1 = p->window_pad + p->width;
-    u.by0 = p->window_pad;
-    u.by1 = p->window_pad + p->height;
+static dfl split_d(double v) { return {(float)v, (float)(v - (double)(float)v)}; }
+
+UpdateDf make_update_df(const abm_vf_params *p, int phi_ok) {
+    UpdateDf u;
+    u.gam = split_d(p->gam);
+    u.v0 = split_d(p->v0);
+    u.alp0 = split_d(p->alp0);
+    u.alp1 = split_d(p->alp1);
+    u.bet0 = split_d(p->bet0);
+    u.bet1 = split_d(p->bet1);
+    u.max_vel = split_d(p->max_vel);
+    u.max_th = split_d(p->max_th);
+    u.dt = split_d(p->dt);
+    u.bx0 = split_d(p->window_pad);
+    u.bx1 = split_d(p->window_pad + p->width);
+    u.by0 = split_d(p->window_pad);
+    u.by1 = split_d(p->window_pad + p->height);
     u.limit = p->limit_movement != 0;
     u.torus = p->boundary == ABM_BOUNDARY_INFINITE;
+    u.phi_ok = phi_ok;
     return u;
 }
 
@@ -791,13 +783,13 @@ int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent) {
     return ABM_OK;
 }
 
-// Launches of one step (pair kernel + update kernel) given the grid tables and the sums
-// buffer; shared by abm_vpf_flock_step and abm_vpf_flock_step_noalloc.
+// Launch of one step given the grid tables and the sincos table; shared by
+// abm_vpf_flock_step, abm_vpf_flock_batched and abm_vpf_flock_step_noalloc.
 static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
                        const abm_vf_params *p, const abm_agent_overrides *ov,
                        uint32_t *vpf_bits_dev, double *terms_dev, unsigned long long *diag_dev,
-                       cudaStream_t s, const GridDev *g, long long *sums, const char *fn,
-                       const int *seg_begin = nullptr, const int *seg_end = nullptr,
+                       cudaStream_t s, const GridDev *g, const float4 *sctab, long long *sums,
+                       const char *fn, const int *seg_begin = nullptr, const int *seg_end = nullptr,
                        const int *order = nullptr) {
     int st;
     int warps, tile, mode, wpa;
@@ -824,9 +816,10 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     a.diag = diag_dev;
     a.W = {(float)p->width, (float)(p->width - (double)(float)p->width)};
     a.H = {(float)p->height, (float)(p->height - (double)(float)p->height)};
-    a.up = make_update(p);
-    a.g = *g;
+    a.ud = make_update_df(p, g->phi_ok);
+    a.sctab = sctab;
     a.sums = sums;
+    a.g = *g;
     a.seg_begin = seg_begin;
     a.seg_end = seg_end;
     a.order = order;
@@ -862,7 +855,9 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
                       : launch_tiled<true, true, false>(a, warps, s);
     }
     if (st) return st;
-    vpf_update_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+    constexpr int kUpd = 64;
+    if (hetero) vpf_update_kernel<true><<<(n + kUpd - 1) / kUpd, kUpd, 0, s>>>(a);
+    else vpf_update_kernel<false><<<(n + kUpd - 1) / kUpd, kUpd, 0, s>>>(a);
     if ((st = check_cuda(cudaGetLastError(), "vpf_update_kernel launch"))) return st;
     return g->phi_ok ? ABM_OK : ABM_WARN_PHI_MISMATCH;
 }
@@ -892,10 +887,12 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     const GridDev *g = grid_for(p->rv, p->fov0, p->fov1, &st);
     if (!g) return st;
     if ((st = ensure_sincos_table())) return st;
-    cudaStream_t s = (cudaStream_t)stream;
-    long long *sums = (long long *)workspace(s, 32 * (size_t)n, &st);
+    const float4 *sctab = sincos_table_dev(&st);
+    if (!sctab) return st;
+    long long *sums = workspace((cudaStream_t)stream, n, &st);
     if (!sums) return st;
-    return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, g, sums, fn);
+    return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev,
+                       (cudaStream_t)stream, g, sctab, sums, fn);
 }
 
 int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32_t n_total,
@@ -911,11 +908,13 @@ int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32
     const GridDev *g = grid_for(p->rv, p->fov0, p->fov1, &st);
     if (!g) return st;
     if ((st = ensure_sincos_table())) return st;
-    cudaStream_t s = (cudaStream_t)stream;
-    long long *sums = (long long *)workspace(s, 32 * (size_t)n_total, &st);
+    const float4 *sctab = sincos_table_dev(&st);
+    if (!sctab) return st;
+    long long *sums = workspace((cudaStream_t)stream, n_total, &st);
     if (!sums) return st;
-    return step_launch(in, out, n_total, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, g, sums,
-                       fn, seg_begin_dev, seg_end_dev, order_dev);
+    return step_launch(in, out, n_total, p, ov, vpf_bits_dev, terms_dev, diag_dev,
+                       (cudaStream_t)stream, g, sctab, sums, fn, seg_begin_dev,
+                       seg_end_dev, order_dev);
 }
 
 int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
@@ -935,6 +934,15 @@ int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, 
     if (!d) return st;
     if ((st = ensure_sincos_table())) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    if (!d->sincos_loaded) {   // set-up: the double-float sincos table into the array
+        std::vector<float> tab;
+        sincos_table_host(tab);
+        st = check_cuda(cudaMemcpy(d->base + kNaSin, tab.data(), tab.size() * sizeof(float),
+                                   cudaMemcpyHostToDevice),
+                        "cudaMemcpy(no-alloc sincos table)");
+        if (st) return st;
+        d->sincos_loaded = true;
+    }
     if (!d->grid_loaded || d->rv != p->rv || d->fov0 != p->fov0 || d->fov1 != p->fov1) {
         // (re)load this grid's tables into the array, ordered on the caller's stream
         GridHostTables t;
@@ -965,7 +973,7 @@ int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, 
         d->grid_loaded = true;
     }
     return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, &d->g,
-                       (long long *)(d->base + kNaSums), fn);
+                       (const float4 *)(d->base + kNaSin), (long long *)(d->base + kNaSums), fn);
 }
 
 int abm_vpf_check_sincos(const float *theta_dev, int32_t n, double *out_dev, void *stream) {

@@ -258,6 +258,20 @@ const GridDev *grid_for_phi(int rv, const double *phi, int *status) {
     return &res.first->second.g;
 }
 
+void sincos_table_host(std::vector<float> &tab) {
+    tab.assign(4 * (size_t)kSinCosTab, 0.f);
+    for (int k = 0; k < kSinCosTab; ++k) {
+        const long double a = (long double)k * 2.0L * 3.14159265358979323846264338327950288L /
+                              (long double)kSinCosTab;
+        const long double c = cosl(a), sn = sinl(a);
+        const float ch = (float)c, sh = (float)sn;
+        tab[4 * k] = ch;
+        tab[4 * k + 1] = (float)(c - (long double)ch);
+        tab[4 * k + 2] = sh;
+        tab[4 * k + 3] = (float)(sn - (long double)sh);
+    }
+}
+
 // cos/sin(k 2pi / kSinCosTab) as double-float pairs in global memory (per device), for
 // kernels outside the translation unit that holds the __constant__ copy.
 const float4 *sincos_table_dev(int *status) {
@@ -271,17 +285,8 @@ const float4 *sincos_table_dev(int *status) {
         *status = ABM_OK;
         return it->second;
     }
-    std::vector<float> tab(4 * (size_t)kSinCosTab);
-    for (int k = 0; k < kSinCosTab; ++k) {
-        const long double a = (long double)k * 2.0L * 3.14159265358979323846264338327950288L /
-                              (long double)kSinCosTab;
-        const long double c = cosl(a), sn = sinl(a);
-        const float ch = (float)c, sh = (float)sn;
-        tab[4 * k] = ch;
-        tab[4 * k + 1] = (float)(c - (long double)ch);
-        tab[4 * k + 2] = sh;
-        tab[4 * k + 3] = (float)(sn - (long double)sh);
-    }
+    std::vector<float> tab;
+    sincos_table_host(tab);
     void *mem = nullptr;
     std::vector<void *> ptrs;
     int st = upload({{tab.data(), tab.size() * sizeof(float)}}, &mem, ptrs);

@@ -27,10 +27,12 @@
  *     raw pixel k, i.e. the pixel order VSWRM integrates (np.flip of the reference's
  *     returned/stored soc_v_field).  Bits >= Rv are zero.
  *   - The library allocates device memory only for its cached lookup tables (one set per
- *     distinct grid: Rv and field of view) and for a per-stream workspace of 32 bytes per
- *     agent that abm_vpf_flock_step uses between its two launches; the first call for a grid,
- *     and a call with more agents than the stream's workspace holds, allocate synchronously,
- *     so make such a call before capturing a CUDA graph.
+ *     distinct grid: Rv and field of view) and for a per-stream workspace of about 32 bytes
+ *     per agent (the VSWRM sums, handed from the step's pair kernel to its update kernel); the
+ *     first call for a grid, and a call with more agents than the stream's workspace holds,
+ *     allocate synchronously, so make such a call before capturing a CUDA graph.  A graph
+ *     captured from a stream uses that stream's workspace: do not replay it concurrently with
+ *     other calls on the same stream.
  */
 #ifndef ABM_VPF_H
 #define ABM_VPF_H
@@ -173,17 +175,18 @@ int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32
  * step, arguments, results and status codes, for callers that cannot call cudaMalloc, such as
  * code running inside another framework's memory pool, a host that has reserved all device
  * memory, or a graph-building layer that must not change the allocation state.  Its scratch
- * (the per-agent VSWRM sums between the two launches, and the lookup tables of one grid) lives
- * in a file-scope device array of about 2.5 MiB that every GPU loading the library holds until
- * the process exits; no cudaMalloc, cudaFree or other allocating routine is called.
+ * (the per-agent VSWRM sums between the two launches, the lookup tables of one grid and the
+ * double-float sincos table) lives in a file-scope device array of about 2.5 MiB that
+ * every GPU loading the library holds until the process exits; no cudaMalloc, cudaFree or other
+ * allocating routine is called.
  * Limits: n <= ABM_NOALLOC_MAX_AGENTS and rv <= ABM_NOALLOC_MAX_RV, larger values return
  * ABM_ERR_INVALID_ARG / ABM_ERR_RV with a message.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) and uploads the grid tables, and a call with a
- * different rv or field of view uploads them again (synchronously from pageable memory), so
- * make the first call, and the first call for each grid, before any stream capture.  Every
- * call shares the one array and it keeps the last call's contents (nothing in it needs to
- * start at zero: each launch overwrites the sums it reads); calls that overlap on the GPU
- * race on it, so serialise them.
+ * array's device address (cudaGetSymbolAddress) and copies the sincos table into it, and a call
+ * with a different rv or field of view copies that grid's tables (synchronously from pageable
+ * memory), so make the first call, and the first call for each grid, before any stream capture.
+ * Every call shares the one array and it keeps the last call's contents (nothing in it needs to
+ * start at zero: each launch overwrites the sums it reads); calls that overlap on the GPU race
+ * on it, so serialise them.
  */
 #define ABM_NOALLOC_MAX_AGENTS 65536
 #define ABM_NOALLOC_MAX_RV 8192
