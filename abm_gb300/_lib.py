@@ -107,6 +107,8 @@ SIGNATURES = [
     ("abm_vpf_get_step_config", c_int32, [c_i32_p, c_i32_p]),
     ("abm_vpf_set_step_mode", c_int32, [c_int32, c_int32]),
     ("abm_vpf_get_step_mode", c_int32, [c_i32_p, c_i32_p]),
+    ("abm_vpf_set_step_split", c_int32, [c_int32]),
+    ("abm_vpf_get_step_split", c_int32, [c_i32_p]),
     ("abm_vpf_check_sincos", c_int32, [c_float_p, c_int32, c_double_p, c_void_p]),
     ("abm_probe_pipe_peak", c_int32,
      [c_int32, c_int32, c_int32, c_int32, c_float_p, c_double_p, c_void_p]),

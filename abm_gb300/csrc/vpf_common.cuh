@@ -375,10 +375,133 @@ __device__ __forceinline__ void raster_fast(uint32_t *vb, int rv, int s, int e) 
 // where w_k are the trapezoid weights of scipy's trapz over PHI and E = dPhi_V_of(V)^2
 // (vf_supcalc.py:257-277: forward circular difference, backward when V[0]=1, V[Rv-1]=0).
 // Uses sum_k w_k f_k V_k = Q[Rv] V[Rv-1] + sum_{j=1..Rv-1} Q[j] (V[j-1] - V[j]) with Q the
-// prefix sums, so only the transitions of V are visited.  Result valid in lane 0.
+// prefix sums, so only the transitions of V are visited.  The warp lists the transitions in
+// `list` (per-warp shared scratch of `cap` >= 32 entries: pixel index | run-start bit 31),
+// ranked by a warp prefix sum of the words' transition counts, then splits the list evenly over
+// the lanes, four entries a lane per round with the table loads issued first: about
+// ceil(transitions / 128) memory latencies per agent.  Result valid in every lane.
+struct IntegralAcc {
+    long long bc = 0, bs = 0, ec = 0, es = 0;
+
+    __device__ __forceinline__ void consume(const uint32_t *list, int count, const GridDev &g,
+                                            int bwd) {
+        const int lane = threadIdx.x & 31;
+        __syncwarp();
+        for (int k0 = 0; k0 < count; k0 += 128) {
+            uint32_t e[4];
+            longlong2 qv[4], cv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = k0 + 32 * u + lane;
+                e[u] = k < count ? list[k] : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                // every listed pixel index is >= 1 (pixel 0 is never a transition)
+                const int j = (int)(e[u] & 0x7fffffffu);
+                qv[u] = j ? __ldg(g.q + j) : make_longlong2(0, 0);
+                cv[u] = j ? __ldg(g.cpt + j - 1 + bwd) : make_longlong2(0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (e[u] >> 31) {   // run starts at j
+                    bc -= qv[u].x;
+                    bs -= qv[u].y;
+                } else {            // run ends at j (or an empty slot: zero)
+                    bc += qv[u].x;
+                    bs += qv[u].y;
+                }
+                ec += cv[u].x;
+                es += cv[u].y;
+            }
+        }
+        __syncwarp();
+    }
+};
+
 __device__ __forceinline__ void warp_integrals(const uint32_t *vb, const GridDev &g,
-                                               long long &bc, long long &bs, long long &ec,
-                                               long long &es) {
+                                               uint32_t *list, int cap, long long &bc,
+                                               long long &bs, long long &ec, long long &es) {
+    const int lane = threadIdx.x & 31;
+    const int rv = g.rv, words = g.words;
+    const uint32_t v0 = vb[0] & 1u;
+    const uint32_t vl = (vb[(rv - 1) >> 5] >> ((rv - 1) & 31)) & 1u;
+    const int bwd = (v0 == 1u && vl == 0u) ? 1 : 0;
+    IntegralAcc acc;
+    int fill = 0;   // entries in the list (warp-uniform)
+    for (int w0 = 0; w0 < words; w0 += 32) {
+        const int w = w0 + lane;
+        uint32_t cur = 0u, D = 0u;
+        if (w < words) {
+            cur = vb[w];
+            const uint32_t prev = w > 0 ? (vb[w - 1] >> 31) : (cur & 1u);
+            D = cur ^ ((cur << 1) | prev);
+            if (w == words - 1 && (rv & 31)) D &= (1u << (rv & 31)) - 1u;
+        }
+        const int c = __popc(D);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(ABM_FULL_MASK, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(ABM_FULL_MASK, incl, 31);
+        const int first = incl - c;   // this lane's first rank within the 32 words
+        for (int done = 0; done < total;) {   // warp-uniform; one pass unless the list fills
+            if (fill == cap) {
+                acc.consume(list, fill, g, bwd);
+                fill = 0;
+            }
+            const int take = min(total - done, cap - fill);
+            uint32_t d = D;
+            if (take == total) {   // the whole pass fits: no rank test
+                int pos = fill + first;
+                while (d) {
+                    const int b = __ffs(d) - 1;
+                    d &= d - 1u;
+                    list[pos++] = (uint32_t)((w << 5) + b) | (((cur >> b) & 1u) << 31);
+                }
+            } else {
+                for (int r = first; d; ++r) {
+                    const int b = __ffs(d) - 1;
+                    d &= d - 1u;
+                    if (r >= done && r < done + take)
+                        list[fill + r - done] = (uint32_t)((w << 5) + b) | (((cur >> b) & 1u) << 31);
+                }
+            }
+            fill += take;
+            done += take;
+        }
+    }
+    acc.consume(list, fill, g, bwd);
+    bc = acc.bc;
+    bs = acc.bs;
+    ec = acc.ec;
+    es = acc.es;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bc += __shfl_xor_sync(ABM_FULL_MASK, bc, o);
+        bs += __shfl_xor_sync(ABM_FULL_MASK, bs, o);
+        ec += __shfl_xor_sync(ABM_FULL_MASK, ec, o);
+        es += __shfl_xor_sync(ABM_FULL_MASK, es, o);
+    }
+    if (vl) {
+        bc += g.qc_total;
+        bs += g.qs_total;
+    }
+    if (v0 != vl) {  // the circular edge between pixels Rv-1 and 0
+        longlong2 cv = g.cpt[bwd ? 0 : rv - 1];
+        ec += cv.x;
+        es += cv.y;
+    }
+}
+
+// The same sums with each lane walking the transitions of its own words one by one (one table
+// latency per transition of the busiest lane).  Fewer instructions than warp_integrals when
+// the bitmask has few transitions per word, as in the small swarms of a batched sweep.
+__device__ __forceinline__ void warp_integrals_loop(const uint32_t *vb, const GridDev &g,
+                                                    long long &bc, long long &bs, long long &ec,
+                                                    long long &es) {
     const int lane = threadIdx.x & 31;
     const int rv = g.rv;
     const uint32_t v0 = vb[0] & 1u;

@@ -37,6 +37,11 @@ struct StepArgs {
     UpdateDf ud;           // the update's parameters in double-float
     const float4 *sctab;   // global copy of the double-float sincos table
     long long *sums;       // n x 4 workspace: bc, bs, ec, es of every agent
+    // split l1 form: block b works on neighbour chunk (b & (2^chunk_shift - 1)) of agent
+    // b >> chunk_shift (chunk_len neighbours, a multiple of 32) and ORs its partial bitmask
+    // into vbits (n x words, zero between steps); NULL for the one-block-per-agent form
+    uint32_t *vbits;
+    int chunk_shift, chunk_len;
     // batched sweeps: agent i sees the agents [seg_begin[i], seg_end[i]) of its instance;
     // block b works on agent order[b] (largest instances first); all NULL for one swarm
     const int *seg_begin, *seg_end, *order;
@@ -46,6 +51,7 @@ static int g_warps = 8;    // tiled form: focal warps per block
 static int g_tile = 8192;  // tiled form: neighbour tile length
 static int g_mode = 0;     // 0 auto, 1 l1, 2 tiled
 static int g_wpa = 1;      // l1 form: warps per focal agent
+static int g_split = 0;    // l1 form: neighbour chunks per agent (0 auto, else a power of two)
 static std::mutex g_cfg_mu;
 
 // cos/sin(k 2pi/1024) as double-float pairs, read with warp-uniform indices (constant cache).
@@ -71,27 +77,50 @@ static int ensure_sincos_table() {
     return st;
 }
 
-// Per-(device, stream) workspace for the per-agent sums handed from the pair kernel to the
-// update kernel (32 B per agent).  A workspace that grows is replaced but the old one stays
-// allocated, since a CUDA graph captured from the stream may still use it.
-static long long *workspace(cudaStream_t stream, int n, int *status) {
+// Per-(device, stream) workspace: the split form's per-agent bitmasks (zero between steps: the
+// finish kernel clears what the pair kernel set) at offset 0, then the per-agent sums handed
+// to the update (32 B per agent).  Zeroed when allocated.  A workspace that grows is replaced
+// but the old one stays allocated, since a CUDA graph captured from the stream may still use
+// it.
+struct Workspace {
+    uint32_t *vbits = nullptr;
+    long long *sums = nullptr;
+};
+
+static Workspace workspace(cudaStream_t stream, int n, int words, int *status) {
+    struct Entry {
+        unsigned char *p = nullptr;
+        long agents = 0;
+        size_t vbits_bytes = 0;
+    };
     static std::mutex mu;
-    static std::map<std::pair<int, void *>, std::pair<void *, long>> ws;
+    static std::map<std::pair<int, void *>, Entry> ws;
     static std::vector<void *> retired;
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
-    auto &e = ws[{dev, (void *)stream}];
-    if (e.second < n) {
-        const long cap = std::max<long>(n, 1024);
-        void *p = nullptr;
-        *status = check_cuda(cudaMalloc(&p, (size_t)cap * 32), "cudaMalloc(step workspace)");
-        if (*status) return nullptr;
-        if (e.first) retired.push_back(e.first);
-        e = {p, cap};
+    Entry &e = ws[{dev, (void *)stream}];
+    const size_t vb_need = ((size_t)n * words * 4 + 255) & ~size_t(255);
+    if (e.agents < n || e.vbits_bytes < vb_need) {
+        Entry ne;
+        ne.agents = std::max<long>({(long)n, e.agents, 1024L});
+        ne.vbits_bytes = std::max(vb_need, e.vbits_bytes);
+        const size_t bytes = ne.vbits_bytes + (size_t)ne.agents * 32;
+        *status = check_cuda(cudaMalloc((void **)&ne.p, bytes), "cudaMalloc(step workspace)");
+        if (*status) return Workspace();
+        *status = check_cuda(cudaMemsetAsync(ne.p, 0, bytes, stream), "cudaMemsetAsync(workspace)");
+        if (*status) {
+            cudaFree(ne.p);
+            return Workspace();
+        }
+        if (e.p) retired.push_back(e.p);
+        e = ne;
     }
     *status = ABM_OK;
-    return (long long *)e.first;
+    Workspace w;
+    w.vbits = (uint32_t *)e.p;
+    w.sums = (long long *)(e.p + e.vbits_bytes);
+    return w;
 }
 
 // Per-warp work queues of the step kernel: candidate neighbours that survived the cull (their
@@ -122,6 +151,10 @@ struct QEntry<true> {
         return QEntry{make_float4(x, y, r, 0.f)};
     }
 };
+
+// Transition-list capacity of a warp's drained queues (both queues, 4 B entries).
+template <bool HETERO>
+constexpr int kListCap = (kQueue + kQueue2) * (int)sizeof(QEntry<HETERO>) / 4;
 
 // ---------------------------------------------------------------------------- no-alloc scratch
 // Scratch of abm_vpf_flock_step_noalloc, for callers that cannot allocate device memory: the
@@ -299,12 +332,14 @@ __device__ __forceinline__ void enqueue_candidate(const FocalDev &f, bool live, 
     }
 }
 
-// Warp epilogue of a focal agent: VSWRM integrals, the optional bitmask output and (lane 0)
-// the sums for the update kernel.
-__device__ __forceinline__ void finish_agent(const StepArgs &a, int i, const uint32_t *vb) {
+// Warp epilogue of a focal agent: VSWRM integrals (listing the transitions in the warp's
+// drained queue space), the optional bitmask output and (lane 0) the sums for the update.
+__device__ __forceinline__ void finish_agent(const StepArgs &a, int i, const uint32_t *vb,
+                                             uint32_t *list, int cap) {
     const int lane = threadIdx.x & 31;
     long long bc, bs, ec, es;
-    warp_integrals(vb, a.g, bc, bs, ec, es);
+    if (a.seg_begin) warp_integrals_loop(vb, a.g, bc, bs, ec, es);   // small batched swarms
+    else warp_integrals(vb, a.g, list, cap, bc, bs, ec, es);
     if (a.bits) {
         uint32_t *dst = a.bits + (size_t)i * a.g.words;
         for (int w = lane; w < a.g.words; w += 32) dst[w] = vb[w];
@@ -338,9 +373,14 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int words = a.g.words;
-    const int i = a.order ? a.order[blockIdx.x] : blockIdx.x;
-    const int j0 = a.seg_begin ? a.seg_begin[i] : 0;
-    const int n = a.seg_end ? a.seg_end[i] : a.n;   // neighbours are [j0, n)
+    const bool split = a.vbits != nullptr;
+    const int i = a.order ? a.order[blockIdx.x] : (blockIdx.x >> a.chunk_shift);
+    int j0 = a.seg_begin ? a.seg_begin[i] : 0;
+    int n = a.seg_end ? a.seg_end[i] : a.n;   // neighbours are [j0, n)
+    if (split) {
+        j0 = (blockIdx.x & ((1 << a.chunk_shift) - 1)) * a.chunk_len;
+        n = min(n, j0 + a.chunk_len);
+    }
     uint32_t *vb = reinterpret_cast<uint32_t *>(smem);
     size_t off = ((size_t)words * 4 + 15) & ~size_t(15);
     QEntry<HETERO> *q = reinterpret_cast<QEntry<HETERO> *>(smem + off) + warp * (kQueue + kQueue2);
@@ -379,8 +419,15 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
                                                   &counters[1]);
     drain_deferred<TORUS, HETERO>(f, q2, q2n, vb, a, &counters[0], &counters[1]);
     if (WPA > 1) __syncthreads(); else __syncwarp();
-    if (warp == 0) {
-        finish_agent(a, i, vb);
+    if (split) {   // partial bitmask into the agent's global one; integrals in the finish kernel
+        uint32_t *gb = a.vbits + (size_t)i * words;
+        for (int w = threadIdx.x; w < words; w += 32 * WPA) {
+            const uint32_t v = vb[w];
+            if (v) atomicOr(gb + w, v);
+        }
+        if (threadIdx.x == 0) flush_counters(a, counters);
+    } else if (warp == 0) {
+        finish_agent(a, i, vb, reinterpret_cast<uint32_t *>(q), kListCap<HETERO>);
         if (lane == 0) flush_counters(a, counters);
     }
 }
@@ -497,13 +544,27 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
                                                       &counters[1]);
         drain_deferred<TORUS, HETERO>(f, q2, q2n, vb, a, &counters[0], &counters[1]);
         __syncwarp();
-        finish_agent(a, i, vb);
+        finish_agent(a, i, vb, reinterpret_cast<uint32_t *>(q), kListCap<HETERO>);
     }
     __syncthreads();
     if (tid == 0) flush_counters(a, counters);
 }
 
 // ---------------------------------------------------------------------------- update kernel
+// New state, optional terms and the non-finite count of agent k.
+__device__ __forceinline__ void store_update(const StepArgs &a, int k, const UpdateOut &o) {
+    a.xo[k] = o.x;
+    a.yo[k] = o.y;
+    a.tho[k] = o.th;
+    a.vo[k] = o.v;
+    if (a.terms) {
+        double *t = a.terms + 6 * (size_t)k;
+        for (int m = 0; m < 6; ++m) t[m] = (double)o.terms[m].hi + (double)o.terms[m].lo;
+    }
+    if (a.diag && !(isfinite(o.x) && isfinite(o.y) && isfinite(o.th) && isfinite(o.v)))
+        atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
+}
+
 // The reference's update of every agent from its sums, one thread per agent.
 template <bool HETERO>
 __global__ void __launch_bounds__(64) vpf_update_kernel(const StepArgs a) {
@@ -517,16 +578,66 @@ __global__ void __launch_bounds__(64) vpf_update_kernel(const StepArgs a) {
     const float R = HETERO ? a.radius[k] : a.radius0;
     const UpdateOut o = update_agent_df(a.ud, a.sctab, a.x[k], a.y[k], a.th[k], a.v[k], R,
                                         s0.x, s0.y, s1.x, s1.y, alp0, bet0, v0);
-    a.xo[k] = o.x;
-    a.yo[k] = o.y;
-    a.tho[k] = o.th;
-    a.vo[k] = o.v;
-    if (a.terms) {
-        double *t = a.terms + 6 * (size_t)k;
-        for (int m = 0; m < 6; ++m) t[m] = (double)o.terms[m].hi + (double)o.terms[m].lo;
+    store_update(a, k, o);
+}
+
+// ---------------------------------------------------------------------------- finish kernel
+// After the split l1 form: one warp per agent stages the agent's bitmask in shared memory,
+// clears the global copy for the next step, writes the optional bitmask output and reduces
+// the VSWRM sums; warp 0 then applies the update to the block's agents, one lane each.
+constexpr int kFinishWarps = 8;
+constexpr int kFinishList = 256;   // transition-list entries per warp
+
+template <bool HETERO>
+__global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const StepArgs a) {
+    extern __shared__ __align__(16) unsigned char fsmem[];
+    __shared__ longlong2 sums[kFinishWarps][2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, words = a.g.words;
+    const int k = blockIdx.x * kFinishWarps + warp;
+    if (k < a.n) {
+        uint32_t *vb = reinterpret_cast<uint32_t *>(fsmem) + warp * words;
+        uint32_t *gb = a.vbits + (size_t)k * words;
+        for (int base = 0; base < words; base += 128) {   // loads first: one latency
+            uint32_t t[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int w = base + 32 * u + lane;
+                t[u] = w < words ? __ldcg(gb + w) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int w = base + 32 * u + lane;
+                if (w < words) {
+                    vb[w] = t[u];
+                    gb[w] = 0u;
+                }
+            }
+        }
+        __syncwarp();
+        uint32_t *list = reinterpret_cast<uint32_t *>(fsmem) + kFinishWarps * words +
+                         warp * kFinishList;
+        long long bc, bs, ec, es;
+        warp_integrals(vb, a.g, list, kFinishList, bc, bs, ec, es);
+        if (a.bits) {
+            uint32_t *dst = a.bits + (size_t)k * words;
+            for (int w = lane; w < words; w += 32) dst[w] = vb[w];
+        }
+        if (lane == 0) {
+            sums[warp][0] = make_longlong2(bc, bs);
+            sums[warp][1] = make_longlong2(ec, es);
+        }
     }
-    if (a.diag && !(isfinite(o.x) && isfinite(o.y) && isfinite(o.th) && isfinite(o.v)))
-        atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
+    __syncthreads();
+    const int ku = blockIdx.x * kFinishWarps + lane;
+    if (warp != 0 || lane >= kFinishWarps || ku >= a.n) return;
+    const longlong2 s0 = sums[lane][0], s1 = sums[lane][1];
+    const dfl alp0 = a.alp0 ? dfl{a.alp0[ku], 0.f} : a.ud.alp0;
+    const dfl bet0 = a.bet0 ? dfl{a.bet0[ku], 0.f} : a.ud.bet0;
+    const dfl v0 = a.v0 ? dfl{a.v0[ku], 0.f} : a.ud.v0;
+    const float R = HETERO ? a.radius[ku] : a.radius0;
+    const UpdateOut o = update_agent_df(a.ud, a.sctab, a.x[ku], a.y[ku], a.th[ku], a.v[ku], R,
+                                        s0.x, s0.y, s1.x, s1.y, alp0, bet0, v0);
+    store_update(a, ku, o);
 }
 
 // Evaluates the in-kernel double-float cos/sin (verification hook for the tests).
@@ -539,12 +650,55 @@ __global__ void check_sincos_kernel(const float *theta, int n, double *out) {
     out[2 * k + 1] = (double)s.hi + (double)s.lo;
 }
 
+// Resident blocks per SM of a kernel at a given block size and dynamic shared memory, times
+// the SM count (cached per device and configuration).
+static int resident_slots(const void *kern, int threads, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void *, int, size_t>, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_tuple(dev, kern, threads, smem);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    int bps = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, threads, smem) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return cache[key] = bps * sms;
+}
+
+// l1 form.  With a.vbits set (a single swarm, bitmask workspace available) each agent's
+// neighbours are split into `split` chunks (0: enough chunks that the blocks fill the GPU about
+// three times over, so the block scheduler balances the SMs' work; chunks of at least 256
+// neighbours); *chunks returns the number used (1: one block per agent, a.vbits unused).
 template <bool TORUS, bool HETERO>
-static int launch_l1(const StepArgs &a, int wpa, cudaStream_t stream) {
+static int launch_l1(StepArgs a, int wpa, int split, cudaStream_t stream, int *chunks) {
     const size_t smem = l1_smem_bytes(wpa, a.g.words, HETERO);
-    if (wpa == 1) vpf_pairs_l1_kernel<TORUS, HETERO, 1><<<a.n, 32, smem, stream>>>(a);
-    else if (wpa == 2) vpf_pairs_l1_kernel<TORUS, HETERO, 2><<<a.n, 64, smem, stream>>>(a);
-    else vpf_pairs_l1_kernel<TORUS, HETERO, 4><<<a.n, 128, smem, stream>>>(a);
+    const void *kern = wpa == 1   ? (const void *)vpf_pairs_l1_kernel<TORUS, HETERO, 1>
+                       : wpa == 2 ? (const void *)vpf_pairs_l1_kernel<TORUS, HETERO, 2>
+                                  : (const void *)vpf_pairs_l1_kernel<TORUS, HETERO, 4>;
+    int c = 1;
+    if (a.vbits) {
+        if (split > 0) {
+            c = split;
+        } else {
+            const long slots = resident_slots(kern, 32 * wpa, smem);
+            while (c < 16 && (long)a.n * c < 3 * slots && a.n / (2 * c) >= 256) c *= 2;
+        }
+    }
+    int shift = 0;
+    while ((1 << shift) < c) ++shift;
+    a.chunk_shift = shift;
+    a.chunk_len = c > 1 ? ((a.n + c - 1) / c + 31) / 32 * 32 : a.n;
+    if (c == 1) a.vbits = nullptr;
+    *chunks = c;
+    const unsigned blocks = (unsigned)a.n << shift;
+    if (wpa == 1) vpf_pairs_l1_kernel<TORUS, HETERO, 1><<<blocks, 32, smem, stream>>>(a);
+    else if (wpa == 2) vpf_pairs_l1_kernel<TORUS, HETERO, 2><<<blocks, 64, smem, stream>>>(a);
+    else vpf_pairs_l1_kernel<TORUS, HETERO, 4><<<blocks, 128, smem, stream>>>(a);
     return check_cuda(cudaGetLastError(), "vpf_pairs_l1_kernel launch");
 }
 
@@ -711,13 +865,16 @@ struct VswrmArgs {
     GridDev g;
 };
 
-__global__ void vswrm_kernel(const VswrmArgs a) {
+constexpr int kVswrmWarps = 8;
+
+__global__ void __launch_bounds__(32 * kVswrmWarps) vswrm_kernel(const VswrmArgs a) {
+    __shared__ uint32_t lists[kVswrmWarps][256];
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= a.n) return;
     const uint32_t *vb = a.bits + (size_t)warp * a.g.words;
     long long bc, bs, ec, es;
-    warp_integrals(vb, a.g, bc, bs, ec, es);
+    warp_integrals(vb, a.g, lists[threadIdx.x >> 5], 256, bc, bs, ec, es);
     if (lane == 0) {
         const double GAM = a.prm[0], ALP1 = a.prm[3], BET1 = a.prm[6];
         const double ALP0 = a.alp0 ? (double)a.alp0[warp] : a.prm[2];
@@ -776,6 +933,20 @@ int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent) {
     return ABM_OK;
 }
 
+int abm_vpf_set_step_split(int32_t chunks) {
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    if (chunks < 0 || chunks > 16 || (chunks & (chunks - 1)))
+        return set_error(ABM_ERR_INVALID_ARG, "chunks=%d", chunks);
+    g_split = chunks;
+    return ABM_OK;
+}
+
+int abm_vpf_get_step_split(int32_t *chunks) {
+    std::lock_guard<std::mutex> lk(g_cfg_mu);
+    if (chunks) *chunks = g_split;
+    return ABM_OK;
+}
+
 int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent) {
     std::lock_guard<std::mutex> lk(g_cfg_mu);
     if (mode) *mode = g_mode;
@@ -788,13 +959,14 @@ int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent) {
 static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
                        const abm_vf_params *p, const abm_agent_overrides *ov,
                        uint32_t *vpf_bits_dev, double *terms_dev, unsigned long long *diag_dev,
-                       cudaStream_t s, const GridDev *g, const float4 *sctab, long long *sums,
-                       const char *fn, const int *seg_begin = nullptr, const int *seg_end = nullptr,
+                       cudaStream_t s, const GridDev *g, const float4 *sctab,
+                       const Workspace &ws, const char *fn, const int *seg_begin = nullptr, const int *seg_end = nullptr,
                        const int *order = nullptr) {
     int st;
-    int warps, tile, mode, wpa;
+    int warps, tile, mode, wpa, split;
     abm_vpf_get_step_config(&warps, &tile);
     abm_vpf_get_step_mode(&mode, &wpa);
+    abm_vpf_get_step_split(&split);
     StepArgs a;
     memset(&a, 0, sizeof(a));
     a.x = in->x;
@@ -818,7 +990,8 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     a.H = {(float)p->height, (float)(p->height - (double)(float)p->height)};
     a.ud = make_update_df(p, g->phi_ok);
     a.sctab = sctab;
-    a.sums = sums;
+    a.sums = ws.sums;
+    a.vbits = seg_begin ? nullptr : ws.vbits;
     a.g = *g;
     a.seg_begin = seg_begin;
     a.seg_end = seg_end;
@@ -828,11 +1001,12 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     // auto: the l1 form while the positions fit comfortably in L1, tiled beyond; segmented
     // (batched) swarms always use the l1 form
     const bool use_l1 = seg_begin || mode == 1 || (mode == 0 && n <= 16384);
+    int chunks = 1;
     if (use_l1) {
-        if (!torus && !hetero) st = launch_l1<false, false>(a, wpa, s);
-        else if (!torus && hetero) st = launch_l1<false, true>(a, wpa, s);
-        else if (torus && !hetero) st = launch_l1<true, false>(a, wpa, s);
-        else st = launch_l1<true, true>(a, wpa, s);
+        if (!torus && !hetero) st = launch_l1<false, false>(a, wpa, split, s, &chunks);
+        else if (!torus && hetero) st = launch_l1<false, true>(a, wpa, split, s, &chunks);
+        else if (torus && !hetero) st = launch_l1<true, false>(a, wpa, split, s, &chunks);
+        else st = launch_l1<true, true>(a, wpa, split, s, &chunks);
     } else {
         a.tile = std::min(tile, ((n + 31) / 32) * 32);
         const long per = (hetero ? 3L : 2L) * 4L;   // bytes per staged neighbour
@@ -855,10 +1029,19 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
                       : launch_tiled<true, true, false>(a, warps, s);
     }
     if (st) return st;
-    constexpr int kUpd = 64;
-    if (hetero) vpf_update_kernel<true><<<(n + kUpd - 1) / kUpd, kUpd, 0, s>>>(a);
-    else vpf_update_kernel<false><<<(n + kUpd - 1) / kUpd, kUpd, 0, s>>>(a);
-    if ((st = check_cuda(cudaGetLastError(), "vpf_update_kernel launch"))) return st;
+    if (chunks > 1) {
+        const int blocks = (n + kFinishWarps - 1) / kFinishWarps;
+        const size_t smem = (size_t)kFinishWarps * (g->words + kFinishList) * sizeof(uint32_t);
+        if (hetero) vpf_finish_kernel<true><<<blocks, 32 * kFinishWarps, smem, s>>>(a);
+        else vpf_finish_kernel<false><<<blocks, 32 * kFinishWarps, smem, s>>>(a);
+        st = check_cuda(cudaGetLastError(), "vpf_finish_kernel launch");
+    } else {
+        constexpr int kUpd = 64;
+        if (hetero) vpf_update_kernel<true><<<(n + kUpd - 1) / kUpd, kUpd, 0, s>>>(a);
+        else vpf_update_kernel<false><<<(n + kUpd - 1) / kUpd, kUpd, 0, s>>>(a);
+        st = check_cuda(cudaGetLastError(), "vpf_update_kernel launch");
+    }
+    if (st) return st;
     return g->phi_ok ? ABM_OK : ABM_WARN_PHI_MISMATCH;
 }
 
@@ -889,10 +1072,10 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     if ((st = ensure_sincos_table())) return st;
     const float4 *sctab = sincos_table_dev(&st);
     if (!sctab) return st;
-    long long *sums = workspace((cudaStream_t)stream, n, &st);
-    if (!sums) return st;
+    const Workspace ws = workspace((cudaStream_t)stream, n, g->words, &st);
+    if (!ws.sums) return st;
     return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev,
-                       (cudaStream_t)stream, g, sctab, sums, fn);
+                       (cudaStream_t)stream, g, sctab, ws, fn);
 }
 
 int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32_t n_total,
@@ -910,10 +1093,10 @@ int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32
     if ((st = ensure_sincos_table())) return st;
     const float4 *sctab = sincos_table_dev(&st);
     if (!sctab) return st;
-    long long *sums = workspace((cudaStream_t)stream, n_total, &st);
-    if (!sums) return st;
+    const Workspace ws = workspace((cudaStream_t)stream, n_total, g->words, &st);
+    if (!ws.sums) return st;
     return step_launch(in, out, n_total, p, ov, vpf_bits_dev, terms_dev, diag_dev,
-                       (cudaStream_t)stream, g, sctab, sums, fn, seg_begin_dev,
+                       (cudaStream_t)stream, g, sctab, ws, fn, seg_begin_dev,
                        seg_end_dev, order_dev);
 }
 
@@ -972,8 +1155,10 @@ int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, 
         d->fov1 = p->fov1;
         d->grid_loaded = true;
     }
+    Workspace na_ws;   // the one-block-per-agent form: no bitmask workspace
+    na_ws.sums = (long long *)(d->base + kNaSums);
     return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, &d->g,
-                       (const float4 *)(d->base + kNaSin), (long long *)(d->base + kNaSums), fn);
+                       (const float4 *)(d->base + kNaSin), na_ws, fn);
 }
 
 int abm_vpf_check_sincos(const float *theta_dev, int32_t n, double *out_dev, void *stream) {
@@ -1063,7 +1248,7 @@ int abm_vswrm_integrals(int32_t n_fields, int32_t rv, const uint32_t *bits_dev,
     a.n = n_fields;
     a.out = out_dev;
     a.g = *g;
-    const int threads = 256;
+    const int threads = 32 * kVswrmWarps;
     const int blocks = (n_fields * 32 + threads - 1) / threads;
     vswrm_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(a);
     return check_cuda(cudaGetLastError(), "vswrm_kernel launch");

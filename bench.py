@@ -487,7 +487,7 @@ def run_gb300(args, rank, world):
                     "d2h_bytes_per_step": 16 * n,
                     "path": "abm_vpf_flock_step via ctypes, pinned host state, H2D + step + "
                             "D2H each step"},
-            "gpu_launches": args.steps,
+            "gpu_launches": 2 * args.steps,   # pair kernel + update (or finish) kernel
             "roofline": roofline, "clocks": clk,
             "wall_s_timed_region": t_wall,
             "diagnostics": diag}

@@ -27,8 +27,8 @@
  *     raw pixel k, i.e. the pixel order VSWRM integrates (np.flip of the reference's
  *     returned/stored soc_v_field).  Bits >= Rv are zero.
  *   - The library allocates device memory only for its cached lookup tables (one set per
- *     distinct grid: Rv and field of view) and for a per-stream workspace of about 32 bytes
- *     per agent (the VSWRM sums, handed from the step's pair kernel to its update kernel); the
+ *     distinct grid: Rv and field of view) and for a per-stream workspace of about 32 + Rv/8
+ *     bytes per agent (the VSWRM sums and the VPF bitmasks handed between the step's kernels); the
  *     first call for a grid, and a call with more agents than the stream's workspace holds,
  *     allocate synchronously, so make such a call before capturing a CUDA graph.  A graph
  *     captured from a stream uses that stream's workspace: do not replay it concurrently with
@@ -287,6 +287,15 @@ int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile);
  * bit-identical results. */
 int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent);
 int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent);
+
+/* Neighbour chunks per focal agent in the L1 form of abm_vpf_flock_step (not the batched or
+ * no-alloc calls): with chunks > 1 each agent's neighbours are split over that many blocks,
+ * whose partial bitmasks are OR-ed into a per-agent bitmask in the stream's workspace (Rv/8
+ * bytes per agent) and reduced by a second kernel, so that the block scheduler can balance the
+ * SMs' work when the swarm alone does not fill the GPU several times over.  0 (the default) =
+ * automatic; otherwise 1, 2, 4, 8 or 16.  All values give bit-identical results. */
+int abm_vpf_set_step_split(int32_t chunks);
+int abm_vpf_get_step_split(int32_t *chunks);
 
 /* Verification hook (no counterpart in the reference): evaluates the double-float cos/sin of
  * float32 headings that the pair kernels use for the focal agent's heading vector.

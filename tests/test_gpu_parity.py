@@ -158,34 +158,88 @@ def test_permutation_invariance_full_size():
         assert np.array_equal(sa[k][perm], sb[k])
 
 
-def test_launch_configs_agree():
-    """Every kernel form and launch configuration gives bit-identical results: the L1 form
-    with 1, 2 and 4 warps per agent, and the TMA-tiled form with several (warps per block,
-    tile) shapes including multi-tile double buffering."""
+def _configs_agree(vp, st, configs, radius=None):
     from abm_gb300 import _lib
-    from abm_gb300.params import VFParams
     from abm_gb300.swarm import VFSwarm
     lib = _lib.load()
-    st = seeded_swarm(5, 1000, 2000.0, 2000.0, R=5.0)
-    vp = VFParams(width=2000.0, height=2000.0, rv=1200, radius=5.0)
     outs = []
     try:
-        for mode, wpa, warps, tile in ((1, 1, 8, 8192), (1, 2, 8, 8192), (1, 4, 8, 8192),
-                                       (2, 1, 8, 2048), (2, 1, 4, 256), (2, 1, 16, 1024),
-                                       (2, 1, 32, 64), (2, 1, 1, 4096)):
+        for mode, wpa, warps, tile, split in configs:
             _lib.check(lib.abm_vpf_set_step_mode(mode, wpa))
             _lib.check(lib.abm_vpf_set_step_config(warps, tile))
-            s = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+            _lib.check(lib.abm_vpf_set_step_split(split))
+            s = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"], radius=radius)
             s.step(want_vpf=True, want_terms=True)
             outs.append((s.vpf_numpy(), s.terms.cpu().numpy(), s.state_numpy()))
     finally:
         lib.abm_vpf_set_step_mode(0, 1)
         lib.abm_vpf_set_step_config(8, 8192)
+        lib.abm_vpf_set_step_split(0)
     for o in outs[1:]:
         assert np.array_equal(o[0], outs[0][0])
         assert np.array_equal(o[1], outs[0][1])
         for k in o[2]:
             assert np.array_equal(o[2][k], outs[0][2][k])
+
+
+def test_launch_configs_agree():
+    """Every kernel form and launch configuration gives bit-identical results: the L1 form
+    with 1, 2 and 4 warps per agent, one block per agent or the neighbours split over 2-16
+    blocks (partial bitmasks OR-ed in the workspace, integrals in the finish kernel), and the
+    TMA-tiled form with several (warps per block, tile) shapes including multi-tile double
+    buffering."""
+    from abm_gb300.params import VFParams
+    st = seeded_swarm(5, 1000, 2000.0, 2000.0, R=5.0)
+    vp = VFParams(width=2000.0, height=2000.0, rv=1200, radius=5.0)
+    _configs_agree(vp, st, ((1, 1, 8, 8192, 1), (1, 2, 8, 8192, 1), (1, 4, 8, 8192, 1),
+                            (1, 1, 8, 8192, 2), (1, 1, 8, 8192, 4), (1, 1, 8, 8192, 16),
+                            (1, 2, 8, 8192, 8), (1, 4, 8, 8192, 4), (0, 1, 8, 8192, 0),
+                            (2, 1, 8, 2048, 0), (2, 1, 4, 256, 0), (2, 1, 16, 1024, 0),
+                            (2, 1, 32, 64, 0), (2, 1, 1, 4096, 0)))
+
+
+def test_launch_configs_agree_torus_radii():
+    """The same agreement on the infinite (torus) arena with per-agent radii."""
+    from abm_gb300.params import VFParams
+    st = seeded_swarm(8, 700, 1500.0, 1500.0, R=5.0)
+    radius = np.random.default_rng(8).uniform(3.0, 9.0, 700).astype(np.float32)
+    vp = VFParams(width=1500.0, height=1500.0, rv=2000, radius=5.0, boundary="infinite")
+    _configs_agree(vp, st, ((1, 1, 8, 8192, 1), (1, 1, 8, 8192, 4), (1, 2, 8, 8192, 16),
+                            (2, 1, 8, 1024, 0)), radius=radius)
+
+
+def test_split_workspace_is_clean_between_calls():
+    """The split form's per-agent bitmasks in the stream workspace are zero again after every
+    step: swarms of different sizes and Rv stepped one after another on one stream give the
+    same results as each stepped first."""
+    from abm_gb300 import _lib
+    from abm_gb300.params import VFParams
+    from abm_gb300.swarm import VFSwarm
+    lib = _lib.load()
+    cases = [(seeded_swarm(11, 900, 1800.0, 1800.0, R=5.0), VFParams(width=1800.0, height=1800.0,
+                                                                    rv=1200, radius=5.0)),
+             (seeded_swarm(12, 300, 900.0, 900.0, R=5.0), VFParams(width=900.0, height=900.0,
+                                                                  rv=3600, radius=5.0)),
+             (seeded_swarm(13, 1500, 2500.0, 2500.0, R=5.0), VFParams(width=2500.0,
+                                                                     height=2500.0, rv=640,
+                                                                     radius=5.0))]
+
+    def run(st, vp):
+        s = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+        s.step(want_vpf=True, want_terms=True)
+        return s.vpf_numpy(), s.terms.cpu().numpy(), s.state_numpy()
+
+    try:
+        _lib.check(lib.abm_vpf_set_step_split(4))
+        first = [run(*c) for c in cases]
+        again = [run(*c) for c in reversed(cases)][::-1]
+    finally:
+        lib.abm_vpf_set_step_split(0)
+    for a, b in zip(first, again):
+        assert np.array_equal(a[0], b[0])
+        assert np.array_equal(a[1], b[1])
+        for k in a[2]:
+            assert np.array_equal(a[2][k], b[2][k])
 
 
 def test_double_float_sincos():
