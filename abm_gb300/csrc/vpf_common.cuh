@@ -376,10 +376,13 @@ __device__ __forceinline__ void raster_fast(uint32_t *vb, int rv, int s, int e) 
 // (vf_supcalc.py:257-277: forward circular difference, backward when V[0]=1, V[Rv-1]=0).
 // Uses sum_k w_k f_k V_k = Q[Rv] V[Rv-1] + sum_{j=1..Rv-1} Q[j] (V[j-1] - V[j]) with Q the
 // prefix sums, so only the transitions of V are visited.  The warp lists the transitions in
-// `list` (per-warp shared scratch of `cap` >= 32 entries: pixel index | run-start bit 31),
-// ranked by a warp prefix sum of the words' transition counts, then splits the list evenly over
-// the lanes, four entries a lane per round with the table loads issued first: about
-// ceil(transitions / 128) memory latencies per agent.  Result valid in every lane.
+// `list` (per-warp shared scratch of `cap` >= 32 entries: pixel index | run-start bit 31):
+// per group of 32 WPL words each lane takes words g0 + lane + 32u (u < WPL), and one warp
+// prefix sum of the lanes' transition counts places every lane's transitions in the list.  The list
+// is then split evenly over the lanes, CW entries a lane per round with the table loads issued
+// first: about ceil(transitions / (32 CW)) memory latencies per agent.  Result valid in every
+// lane.
+template <int CW>
 struct IntegralAcc {
     long long bc = 0, bs = 0, ec = 0, es = 0;
 
@@ -387,23 +390,23 @@ struct IntegralAcc {
                                             int bwd) {
         const int lane = threadIdx.x & 31;
         __syncwarp();
-        for (int k0 = 0; k0 < count; k0 += 128) {
-            uint32_t e[4];
-            longlong2 qv[4], cv[4];
+        for (int k0 = 0; k0 < count; k0 += 32 * CW) {
+            uint32_t e[CW];
+            longlong2 qv[CW], cv[CW];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < CW; ++u) {
                 const int k = k0 + 32 * u + lane;
                 e[u] = k < count ? list[k] : 0u;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < CW; ++u) {
                 // every listed pixel index is >= 1 (pixel 0 is never a transition)
                 const int j = (int)(e[u] & 0x7fffffffu);
                 qv[u] = j ? __ldg(g.q + j) : make_longlong2(0, 0);
                 cv[u] = j ? __ldg(g.cpt + j - 1 + bwd) : make_longlong2(0, 0);
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < CW; ++u) {
                 if (e[u] >> 31) {   // run starts at j
                     bc -= qv[u].x;
                     bs -= qv[u].y;
@@ -419,6 +422,7 @@ struct IntegralAcc {
     }
 };
 
+template <int CW = 4, int WPL = 1>
 __device__ __forceinline__ void warp_integrals(const uint32_t *vb, const GridDev &g,
                                                uint32_t *list, int cap, long long &bc,
                                                long long &bs, long long &ec, long long &es) {
@@ -427,18 +431,24 @@ __device__ __forceinline__ void warp_integrals(const uint32_t *vb, const GridDev
     const uint32_t v0 = vb[0] & 1u;
     const uint32_t vl = (vb[(rv - 1) >> 5] >> ((rv - 1) & 31)) & 1u;
     const int bwd = (v0 == 1u && vl == 0u) ? 1 : 0;
-    IntegralAcc acc;
+    IntegralAcc<CW> acc;
     int fill = 0;   // entries in the list (warp-uniform)
-    for (int w0 = 0; w0 < words; w0 += 32) {
-        const int w = w0 + lane;
-        uint32_t cur = 0u, D = 0u;
-        if (w < words) {
-            cur = vb[w];
-            const uint32_t prev = w > 0 ? (vb[w - 1] >> 31) : (cur & 1u);
-            D = cur ^ ((cur << 1) | prev);
-            if (w == words - 1 && (rv & 31)) D &= (1u << (rv & 31)) - 1u;
+    for (int g0 = 0; g0 < words; g0 += 32 * WPL) {
+        uint32_t cur[WPL], D[WPL];
+        int c = 0;
+#pragma unroll
+        for (int u = 0; u < WPL; ++u) {
+            const int w = g0 + 32 * u + lane;
+            cur[u] = 0u;
+            D[u] = 0u;
+            if (w < words) {
+                cur[u] = vb[w];
+                const uint32_t prev = w > 0 ? (vb[w - 1] >> 31) : (cur[u] & 1u);
+                D[u] = cur[u] ^ ((cur[u] << 1) | prev);
+                if (w == words - 1 && (rv & 31)) D[u] &= (1u << (rv & 31)) - 1u;
+            }
+            c += __popc(D[u]);
         }
-        const int c = __popc(D);
         int incl = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -446,27 +456,33 @@ __device__ __forceinline__ void warp_integrals(const uint32_t *vb, const GridDev
             if (lane >= o) incl += t;
         }
         const int total = __shfl_sync(ABM_FULL_MASK, incl, 31);
-        const int first = incl - c;   // this lane's first rank within the 32 words
+        const int first = incl - c;   // this lane's first rank within the group
         for (int done = 0; done < total;) {   // warp-uniform; one pass unless the list fills
             if (fill == cap) {
                 acc.consume(list, fill, g, bwd);
                 fill = 0;
             }
             const int take = min(total - done, cap - fill);
-            uint32_t d = D;
-            if (take == total) {   // the whole pass fits: no rank test
+            if (take == total) {   // the whole group fits: no rank test
                 int pos = fill + first;
-                while (d) {
-                    const int b = __ffs(d) - 1;
-                    d &= d - 1u;
-                    list[pos++] = (uint32_t)((w << 5) + b) | (((cur >> b) & 1u) << 31);
+#pragma unroll
+                for (int u = 0; u < WPL; ++u) {
+                    const uint32_t base = (uint32_t)(g0 + 32 * u + lane) << 5;
+                    for (uint32_t d = D[u]; d; d &= d - 1u) {
+                        const int b = __ffs(d) - 1;
+                        list[pos++] = (base + b) | (((cur[u] >> b) & 1u) << 31);
+                    }
                 }
             } else {
-                for (int r = first; d; ++r) {
-                    const int b = __ffs(d) - 1;
-                    d &= d - 1u;
-                    if (r >= done && r < done + take)
-                        list[fill + r - done] = (uint32_t)((w << 5) + b) | (((cur >> b) & 1u) << 31);
+                int r = first;
+#pragma unroll
+                for (int u = 0; u < WPL; ++u) {
+                    const uint32_t base = (uint32_t)(g0 + 32 * u + lane) << 5;
+                    for (uint32_t d = D[u]; d; d &= d - 1u, ++r) {
+                        const int b = __ffs(d) - 1;
+                        if (r >= done && r < done + take)
+                            list[fill + r - done] = (base + b) | (((cur[u] >> b) & 1u) << 31);
+                    }
                 }
             }
             fill += take;

@@ -152,6 +152,17 @@ struct QEntry<true> {
     }
 };
 
+// Programmatic dependent launch: the pair kernels let the step's second kernel launch early
+// (it is launched with programmatic stream serialisation); the second kernel prefetches the
+// step's inputs, then waits for the pair kernel's completion and memory flush before it reads
+// anything the pair kernel wrote.
+__device__ __forceinline__ void allow_dependent_launch() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void wait_primary_grid() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Transition-list capacity of a warp's drained queues (both queues, 4 B entries).
 template <bool HETERO>
 constexpr int kListCap = (kQueue + kQueue2) * (int)sizeof(QEntry<HETERO>) / 4;
@@ -390,6 +401,7 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
 
     for (int w = threadIdx.x; w < words; w += 32 * WPA) vb[w] = 0u;
     if (threadIdx.x < 4) counters[threadIdx.x] = 0u;
+    allow_dependent_launch();
     const FocalDev f = load_focal<HETERO>(a, i);
     const float cull_r2 = f.r * f.r * a.g.cull;
     if (WPA > 1) __syncthreads(); else __syncwarp();
@@ -468,6 +480,7 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
 
     const int i = blockIdx.x * nw + warp;
     const bool active = i < n;
+    allow_dependent_launch();
     if (tid < 4) counters[tid] = 0u;
     for (int w = lane; w < words; w += 32) vb[w] = 0u;
     if (TMA && tid == 0) {
@@ -569,15 +582,26 @@ __device__ __forceinline__ void store_update(const StepArgs &a, int k, const Upd
 template <bool HETERO>
 __global__ void __launch_bounds__(64) vpf_update_kernel(const StepArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n) return;
+    const bool live = k < a.n;
+    // inputs of the step (not written by the pair kernel): loaded before the wait
+    float x = 0.f, y = 0.f, th = 0.f, v = 0.f, R = a.radius0;
+    dfl alp0 = a.ud.alp0, bet0 = a.ud.bet0, v0 = a.ud.v0;
+    if (live) {
+        x = a.x[k];
+        y = a.y[k];
+        th = a.th[k];
+        v = a.v[k];
+        if (HETERO) R = a.radius[k];
+        if (a.alp0) alp0 = dfl{a.alp0[k], 0.f};
+        if (a.bet0) bet0 = dfl{a.bet0[k], 0.f};
+        if (a.v0) v0 = dfl{a.v0[k], 0.f};
+    }
+    wait_primary_grid();
+    if (!live) return;
     const longlong2 *sp = reinterpret_cast<const longlong2 *>(a.sums) + 2 * (size_t)k;
-    const longlong2 s0 = sp[0], s1 = sp[1];
-    const dfl alp0 = a.alp0 ? dfl{a.alp0[k], 0.f} : a.ud.alp0;
-    const dfl bet0 = a.bet0 ? dfl{a.bet0[k], 0.f} : a.ud.bet0;
-    const dfl v0 = a.v0 ? dfl{a.v0[k], 0.f} : a.ud.v0;
-    const float R = HETERO ? a.radius[k] : a.radius0;
-    const UpdateOut o = update_agent_df(a.ud, a.sctab, a.x[k], a.y[k], a.th[k], a.v[k], R,
-                                        s0.x, s0.y, s1.x, s1.y, alp0, bet0, v0);
+    const longlong2 s0 = __ldcg(sp), s1 = __ldcg(sp + 1);
+    const UpdateOut o = update_agent_df(a.ud, a.sctab, x, y, th, v, R, s0.x, s0.y, s1.x, s1.y,
+                                        alp0, bet0, v0);
     store_update(a, k, o);
 }
 
@@ -588,13 +612,34 @@ __global__ void __launch_bounds__(64) vpf_update_kernel(const StepArgs a) {
 constexpr int kFinishWarps = 8;
 constexpr int kFinishList = 256;   // transition-list entries per warp
 
+struct FinishInputs {   // one agent's update inputs, parked in shared memory
+    float x, y, th, v, R, alp0, bet0, v0;
+};
+
 template <bool HETERO>
 __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const StepArgs a) {
     extern __shared__ __align__(16) unsigned char fsmem[];
     __shared__ longlong2 sums[kFinishWarps][2];
+    __shared__ FinishInputs uin[kFinishWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, words = a.g.words;
     const int k = blockIdx.x * kFinishWarps + warp;
+    const int ku = blockIdx.x * kFinishWarps + lane;
+    const bool updater = warp == 0 && lane < kFinishWarps && ku < a.n;
     if (k < a.n) {
+        // warp 0 also loads the block's update inputs, so that their latency overlaps the
+        // bitmask loads; they wait in shared memory until the sums are ready
+        FinishInputs in{};
+        if (updater) {
+            in.x = a.x[ku];
+            in.y = a.y[ku];
+            in.th = a.th[ku];
+            in.v = a.v[ku];
+            in.R = HETERO ? a.radius[ku] : a.radius0;
+            in.alp0 = a.alp0 ? a.alp0[ku] : 0.f;
+            in.bet0 = a.bet0 ? a.bet0[ku] : 0.f;
+            in.v0 = a.v0 ? a.v0[ku] : 0.f;
+        }
+        wait_primary_grid();
         uint32_t *vb = reinterpret_cast<uint32_t *>(fsmem) + warp * words;
         uint32_t *gb = a.vbits + (size_t)k * words;
         for (int base = 0; base < words; base += 128) {   // loads first: one latency
@@ -613,11 +658,12 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
                 }
             }
         }
+        if (updater) uin[lane] = in;
         __syncwarp();
         uint32_t *list = reinterpret_cast<uint32_t *>(fsmem) + kFinishWarps * words +
                          warp * kFinishList;
         long long bc, bs, ec, es;
-        warp_integrals(vb, a.g, list, kFinishList, bc, bs, ec, es);
+        warp_integrals<8, 4>(vb, a.g, list, kFinishList, bc, bs, ec, es);
         if (a.bits) {
             uint32_t *dst = a.bits + (size_t)k * words;
             for (int w = lane; w < words; w += 32) dst[w] = vb[w];
@@ -628,15 +674,14 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
         }
     }
     __syncthreads();
-    const int ku = blockIdx.x * kFinishWarps + lane;
-    if (warp != 0 || lane >= kFinishWarps || ku >= a.n) return;
+    if (!updater) return;
+    const FinishInputs in = uin[lane];
     const longlong2 s0 = sums[lane][0], s1 = sums[lane][1];
-    const dfl alp0 = a.alp0 ? dfl{a.alp0[ku], 0.f} : a.ud.alp0;
-    const dfl bet0 = a.bet0 ? dfl{a.bet0[ku], 0.f} : a.ud.bet0;
-    const dfl v0 = a.v0 ? dfl{a.v0[ku], 0.f} : a.ud.v0;
-    const float R = HETERO ? a.radius[ku] : a.radius0;
-    const UpdateOut o = update_agent_df(a.ud, a.sctab, a.x[ku], a.y[ku], a.th[ku], a.v[ku], R,
-                                        s0.x, s0.y, s1.x, s1.y, alp0, bet0, v0);
+    const dfl alp0 = a.alp0 ? dfl{in.alp0, 0.f} : a.ud.alp0;
+    const dfl bet0 = a.bet0 ? dfl{in.bet0, 0.f} : a.ud.bet0;
+    const dfl v0 = a.v0 ? dfl{in.v0, 0.f} : a.ud.v0;
+    const UpdateOut o = update_agent_df(a.ud, a.sctab, in.x, in.y, in.th, in.v, in.R, s0.x,
+                                        s0.y, s1.x, s1.y, alp0, bet0, v0);
     store_update(a, ku, o);
 }
 
@@ -648,6 +693,23 @@ __global__ void check_sincos_kernel(const float *theta, int n, double *out) {
     df_sincos(theta[k], c_sincos, c, s);
     out[2 * k] = (double)c.hi + (double)c.lo;
     out[2 * k + 1] = (double)s.hi + (double)s.lo;
+}
+
+// Launch of the step's second kernel after the pair kernel with programmatic stream
+// serialisation (it may start while the pair kernel drains; it waits in griddepcontrol.wait).
+static cudaError_t launch_dependent(void (*kern)(StepArgs), int blocks, int threads, size_t smem,
+                                    cudaStream_t s, const StepArgs &a) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a);
 }
 
 // Resident blocks per SM of a kernel at a given block size and dynamic shared memory, times
@@ -874,7 +936,7 @@ __global__ void __launch_bounds__(32 * kVswrmWarps) vswrm_kernel(const VswrmArgs
     if (warp >= a.n) return;
     const uint32_t *vb = a.bits + (size_t)warp * a.g.words;
     long long bc, bs, ec, es;
-    warp_integrals(vb, a.g, lists[threadIdx.x >> 5], 256, bc, bs, ec, es);
+    warp_integrals<8, 4>(vb, a.g, lists[threadIdx.x >> 5], 256, bc, bs, ec, es);
     if (lane == 0) {
         const double GAM = a.prm[0], ALP1 = a.prm[3], BET1 = a.prm[6];
         const double ALP0 = a.alp0 ? (double)a.alp0[warp] : a.prm[2];
@@ -1032,14 +1094,16 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     if (chunks > 1) {
         const int blocks = (n + kFinishWarps - 1) / kFinishWarps;
         const size_t smem = (size_t)kFinishWarps * (g->words + kFinishList) * sizeof(uint32_t);
-        if (hetero) vpf_finish_kernel<true><<<blocks, 32 * kFinishWarps, smem, s>>>(a);
-        else vpf_finish_kernel<false><<<blocks, 32 * kFinishWarps, smem, s>>>(a);
-        st = check_cuda(cudaGetLastError(), "vpf_finish_kernel launch");
+        st = check_cuda(launch_dependent(hetero ? vpf_finish_kernel<true>
+                                                : vpf_finish_kernel<false>,
+                                         blocks, 32 * kFinishWarps, smem, s, a),
+                        "vpf_finish_kernel launch");
     } else {
         constexpr int kUpd = 64;
-        if (hetero) vpf_update_kernel<true><<<(n + kUpd - 1) / kUpd, kUpd, 0, s>>>(a);
-        else vpf_update_kernel<false><<<(n + kUpd - 1) / kUpd, kUpd, 0, s>>>(a);
-        st = check_cuda(cudaGetLastError(), "vpf_update_kernel launch");
+        st = check_cuda(launch_dependent(hetero ? vpf_update_kernel<true>
+                                                : vpf_update_kernel<false>,
+                                         (n + kUpd - 1) / kUpd, kUpd, 0, s, a),
+                        "vpf_update_kernel launch");
     }
     if (st) return st;
     return g->phi_ok ? ABM_OK : ABM_WARN_PHI_MISMATCH;
