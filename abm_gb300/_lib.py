@@ -61,6 +61,14 @@ class AbmAgentOverrides(ctypes.Structure):
                 ("v0", c_float_p)]
 
 
+class AbmStepConfig(ctypes.Structure):
+    _fields_ = [("mode", c_int32), ("warps_per_agent", c_int32), ("chunks", c_int32),
+                ("warps_per_block", c_int32), ("tile", c_int32), ("ms_per_step", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # (name, restype, argtypes) of every exported entry point of include/abm_vpf.h
 SIGNATURES = [
     ("abm_vpf_abi_version", c_int32, []),
@@ -109,6 +117,11 @@ SIGNATURES = [
     ("abm_vpf_get_step_mode", c_int32, [c_i32_p, c_i32_p]),
     ("abm_vpf_set_step_split", c_int32, [c_int32]),
     ("abm_vpf_get_step_split", c_int32, [c_i32_p]),
+    ("abm_vpf_autotune", c_int32,
+     [ctypes.POINTER(AbmSwarmState), c_int32, c_i32_p, c_i32_p, c_i32_p,
+      ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_int32,
+      ctypes.POINTER(AbmStepConfig), ctypes.POINTER(AbmStepConfig), c_int32, c_i32_p,
+      ctypes.c_void_p]),
     ("abm_vpf_check_sincos", c_int32, [c_float_p, c_int32, c_double_p, c_void_p]),
     ("abm_probe_pipe_peak", c_int32,
      [c_int32, c_int32, c_int32, c_int32, c_float_p, c_double_p, c_void_p]),

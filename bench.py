@@ -222,18 +222,33 @@ BATCHED = dict(workload="vf_batched_sweep", n_instances=512, n_per_instance="uni
                arena=[1000.0, 1000.0], boundary="walls", steps=2000, graph_chunk=100, seed=3)
 
 
+def compact_table(tried):
+    """[mode, warps per agent, chunks, agents per block, tile, us per step] per candidate."""
+    return {"columns": ["mode", "warps_per_agent", "chunks", "warps_per_block", "tile",
+                        "us_per_step"],
+            "rows": [[t["mode"], t["warps_per_agent"], t["chunks"], t["warps_per_block"],
+                      t["tile"], round(t["ms_per_step"] * 1e3, 2)] for t in tried]}
+
+
+# the library's default step configuration: automatic form and neighbour chunks
+DEFAULT_STEP_CONFIG = {"mode": 0, "warps_per_agent": 1, "warps_per_block": 8, "tile": 8192,
+                       "chunks": 0}
+
+
 def batched_leg(torch, lib, stream, steps=BATCHED["steps"], flush=None):
     """Batched sweep: 512 instances advanced by one abm_vpf_flock_batched call per step,
     captured in CUDA graphs of 100 steps; compared with per-instance abm_vpf_flock_step calls
     (eager, and captured as a graph of 512 x 2 launches per step)."""
     import ctypes
     from abm_gb300 import _lib
+    from abm_gb300 import autotune
     from abm_gb300.batched import BatchedSweep, sweep_instances
     from abm_gb300.params import VFParams
     vp = VFParams(gam=0.1, v0=1.0, alp1=0.08, bet1=0.08, width=1000.0, height=1000.0,
                   rv=BATCHED["rv"], radius=BATCHED["radius"])
     inst = sweep_instances(n_instances=BATCHED["n_instances"], seed=BATCHED["seed"])
     b = BatchedSweep(vp, inst)
+    tuned = autotune.tune(b, reps=3)     # warps per agent of the segmented L1 form
     chunk = BATCHED["graph_chunk"]
     b.capture(chunk)
     b.run(chunk, chunk=chunk)                       # warm-up replay
@@ -272,6 +287,7 @@ def batched_leg(torch, lib, stream, steps=BATCHED["steps"], flush=None):
                                               ctypes.byref(cp), ctypes.byref(ov), None, None,
                                               None, ctypes.c_void_p(s.cuda_stream)))
 
+    autotune.apply(DEFAULT_STEP_CONFIG)     # per-instance launches: the automatic choice
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
@@ -311,7 +327,8 @@ def batched_leg(torch, lib, stream, steps=BATCHED["steps"], flush=None):
                                       "ms_per_step_eager": t_eager * 1e3,
                                       "ms_per_step_graph": t_graph * 1e3,
                                       "launches_per_step": 2 * BATCHED["n_instances"]},
-            "speedup_vs_per_instance_graph": t_graph / per_step}
+            "speedup_vs_per_instance_graph": t_graph / per_step,
+            "autotune": {"best": tuned["best"], "table": compact_table(tuned["tried"])}}
 
 
 # ---------------------------------------------------------------------- differentiable leg
@@ -398,6 +415,8 @@ def run_gb300(args, rank, world):
     n = len(state["x"])
     sw = VFSwarm(params, state["x"], state["y"], state["theta"], state["v"], device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    from abm_gb300 import autotune
+    tuned = autotune.tune(sw, reps=5)   # launch configuration of the step, before any timing
 
     peaks = measure_peaks(lib, torch, stream)
     for _ in range(args.warmup):
@@ -491,6 +510,9 @@ def run_gb300(args, rank, world):
                             "D2H each step"},
             "gpu_launches": 2 * args.steps,   # pair kernel + update (or finish) kernel
             "roofline": roofline, "clocks": clk,
+            "launch_config": dict(tuned["best"], chosen_by="abm_vpf_autotune, 5 steps per "
+                                  "candidate", candidates=len(tuned["tried"]),
+                                  table=compact_table(tuned["tried"])),
             "wall_s_timed_region": t_wall,
             "diagnostics": diag}
     if not args.no_batched:

@@ -297,6 +297,35 @@ int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent);
 int abm_vpf_set_step_split(int32_t chunks);
 int abm_vpf_get_step_split(int32_t *chunks);
 
+/* One launch configuration of the step and its measured time. */
+typedef struct {
+    int32_t mode;              /* 1 = L1 form, 2 = tiled form */
+    int32_t warps_per_agent;   /* L1 form: warps sharing one focal agent (1, 2, 4) */
+    int32_t chunks;            /* L1 form, single swarm: neighbour chunks per agent (1..16) */
+    int32_t warps_per_block;   /* tiled form: focal agents per block */
+    int32_t tile;              /* tiled form: neighbour tile length */
+    float ms_per_step;         /* mean device time of one step; < 0 if the form was refused */
+} abm_step_config;
+
+/*
+ * Autotuner (no counterpart in the reference): times the step on the caller's own state and
+ * stream under every candidate configuration and applies the fastest one through
+ * abm_vpf_set_step_mode / _config / _split.  Candidates for a single swarm (seg_begin_dev ==
+ * NULL): the L1 form with warps_per_agent in {1, 2, 4} x chunks in {1, 2, 4, 8, 16}, and the
+ * tiled form with warps_per_block in {4, 8, 16} x tile in {1024, 2048, 4096, 8192}; for a
+ * batched sweep (segment arrays as for abm_vpf_flock_batched): the L1 form with
+ * warps_per_agent in {1, 2, 4}.  Each candidate runs one untimed step and then `reps` timed
+ * steps (CUDA events on `stream`) from `in` into a scratch state allocated by the call.  All
+ * configurations give bit-identical results, so tuning changes only the speed.  Synchronises
+ * the stream; must not be called during stream capture.  best: the chosen configuration;
+ * tried (nullable, room for max_tried entries) and *n_tried (nullable): every candidate.
+ */
+int abm_vpf_autotune(const abm_swarm_state *in, int32_t n, const int32_t *seg_begin_dev,
+                     const int32_t *seg_end_dev, const int32_t *order_dev,
+                     const abm_vf_params *p, const abm_agent_overrides *ov, int32_t reps,
+                     abm_step_config *best, abm_step_config *tried, int32_t max_tried,
+                     int32_t *n_tried, void *stream);
+
 /* Verification hook (no counterpart in the reference): evaluates the double-float cos/sin of
  * float32 headings that the pair kernels use for the focal agent's heading vector.
  * out_dev: n x 2 doubles (cos, sin). */

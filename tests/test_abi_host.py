@@ -129,3 +129,31 @@ def test_params_from_env_gamma_quirk():
     assert p.alp0 == 2.0 and p.boundary == "infinite"
     assert p.rv == 2400          # vf_sims.py:40-44 rescales Rv by 1/fov_ratio
     assert p.fov == (-0.5 * math.pi, 0.5 * math.pi)
+
+
+def test_step_split_and_autotune_validation(lib):
+    """Chunk counts other than 0 or a power of two up to 16 are refused; the autotuner
+    rejects bad arguments before any CUDA call."""
+    from abm_gb300 import _lib
+    from abm_gb300.params import VFParams
+    for bad in (-1, 3, 32):
+        assert lib.abm_vpf_set_step_split(bad) == _lib.ABM_ERR_INVALID_ARG
+    c = ctypes.c_int32()
+    assert lib.abm_vpf_get_step_split(ctypes.byref(c)) == 0 and c.value in (0, 1, 2, 4, 8, 16)
+    p = VFParams(rv=1200).to_c()
+    st = _lib.AbmSwarmState()
+    best = _lib.AbmStepConfig()
+    seg = (ctypes.c_int32 * 2)()
+    segp = ctypes.cast(seg, _lib.c_i32_p)
+    calls = [  # (in, n, seg_begin, seg_end, params, reps, best)
+        (None, 10, None, None, p, 3, best),
+        (st, 0, None, None, p, 3, best),
+        (st, 10, None, None, p, 0, best),
+        (st, 10, segp, None, p, 3, best),
+        (st, 10, None, None, p, 3, None),
+    ]
+    for s_in, n, sb, se, prm, reps, b in calls:
+        r = lib.abm_vpf_autotune(ctypes.byref(s_in) if s_in is not None else None, n, sb, se,
+                                 None, ctypes.byref(prm), None, reps,
+                                 ctypes.byref(b) if b is not None else None, None, 0, None, None)
+        assert r == _lib.ABM_ERR_INVALID_ARG
