@@ -69,7 +69,49 @@ class AbmStepConfig(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-# (name, restype, argtypes) of every exported entry point of include/abm_vpf.h
+class AbmForageParams(ctypes.Structure):
+    """abm_forage_params of include/abm_forage.h."""
+    _fields_ = ([(k, ctypes.c_double) for k in ("T_w", "Eps_w", "g_w", "B_w", "w_max", "T_u",
+                                                "Eps_u", "g_u", "B_u", "u_max", "S_wu",
+                                                "S_uw", "F_N", "F_R")]
+                + [("Tau", c_int32)]
+                + [(k, ctypes.c_double) for k in ("exp_vel_max", "exp_theta_min",
+                                                  "exp_theta_max", "reloc_theta_max",
+                                                  "exp_stop_ratio", "width", "height",
+                                                  "window_pad", "agent_radius", "consumption")]
+                + [(k, c_int32) for k in ("pooling_time", "teleport_exploit",
+                                          "regenerate_patches", "allow_border_patch_overlap",
+                                          "min_resc_units", "max_resc_units")]
+                + [(k, ctypes.c_double) for k in ("min_resc_quality", "max_resc_quality",
+                                                  "patch_radius")]
+                + [("rv", c_int32)]
+                + [(k, ctypes.c_double) for k in ("fov0", "fov1", "vision_range")]
+                + [(k, c_int32) for k in ("visual_exclusion", "patchwise_exclusion")]
+                + [("seed", ctypes.c_uint64)])
+
+
+# (field, pointer type) of abm_forager_state / abm_patch_state, in declaration order
+FORAGER_FIELDS = (("x", c_float_p), ("y", c_float_p), ("theta", c_float_p), ("v", c_float_p),
+                  ("w", c_double_p), ("u", c_double_p), ("collected", c_double_p),
+                  ("collected_before", c_double_p), ("mode", c_i32_p),
+                  ("override_mode", c_i32_p), ("env_status", c_i32_p),
+                  ("env_status_before", c_i32_p), ("pool_success", c_i32_p),
+                  ("patch_id", c_i32_p), ("novelty", c_u32_p), ("draws", c_u64_p))
+PATCH_FIELDS = (("x", c_double_p), ("y", c_double_p), ("radius", c_double_p),
+                ("units", c_double_p), ("left", c_double_p), ("quality", c_double_p),
+                ("id", c_i32_p), ("draws", c_u64_p))
+
+
+class AbmForagerState(ctypes.Structure):
+    _fields_ = list(FORAGER_FIELDS)
+
+
+class AbmPatchState(ctypes.Structure):
+    _fields_ = list(PATCH_FIELDS)
+
+
+# (name, restype, argtypes) of every exported entry point of include/abm_vpf.h and
+# include/abm_forage.h
 SIGNATURES = [
     ("abm_vpf_abi_version", c_int32, []),
     ("abm_last_error_string", ctypes.c_char_p, []),
@@ -117,6 +159,12 @@ SIGNATURES = [
     ("abm_vpf_get_step_mode", c_int32, [c_i32_p, c_i32_p]),
     ("abm_vpf_set_step_split", c_int32, [c_int32]),
     ("abm_vpf_get_step_split", c_int32, [c_i32_p]),
+    ("abm_forage_params_default", c_int32, [ctypes.POINTER(AbmForageParams)]),
+    ("abm_forage_step", c_int32,
+     [ctypes.POINTER(AbmForagerState), c_int32, ctypes.POINTER(AbmPatchState), c_int32,
+      ctypes.POINTER(AbmForageParams), c_u32_p, c_i32_p, c_double_p, c_u64_p, ctypes.c_void_p]),
+    ("abm_philox4x32", None, [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                              ctypes.POINTER(ctypes.c_uint32)]),
     ("abm_vpf_autotune", c_int32,
      [ctypes.POINTER(AbmSwarmState), c_int32, c_i32_p, c_i32_p, c_i32_p,
       ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_int32,

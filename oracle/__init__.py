@@ -248,3 +248,43 @@ def social_vpf(i, x, y, radii, theta, exploit, patch, vision_range, visual_exclu
                          1 if visual_exclusion else 0, 1 if patchwise else 0, int(rv),
                          float(fov[0]), float(fov[1]), _dp(out))
     return out
+
+
+_FORAGER = (("x", np.float32), ("y", np.float32), ("theta", np.float32), ("v", np.float32),
+            ("w", np.float64), ("u", np.float64), ("collected", np.float64),
+            ("collected_before", np.float64), ("mode", np.int32), ("override_mode", np.int32),
+            ("env_status", np.int32), ("env_status_before", np.int32),
+            ("pool_success", np.int32), ("patch_id", np.int32), ("novelty", np.uint32),
+            ("draws", np.uint64))
+_PATCH = (("x", np.float64), ("y", np.float64), ("radius", np.float64), ("units", np.float64),
+          ("left", np.float64), ("quality", np.float64), ("id", np.int32),
+          ("draws", np.uint64))
+
+
+def forage_step(agents, patches, fp, ip, seed, uniforms=None):
+    """Oracle twin of abm_forage_step: returns (agents, patches, soc (n, rv) float64 stored
+    order, failed regenerations); inputs are not modified.  fp, ip, seed: the arrays of
+    ForageParams.oracle_arrays()."""
+    a = {k: np.array(agents[k], dt, copy=True) for k, dt in _FORAGER}
+    p = {k: np.array(patches[k], dt, copy=True) for k, dt in _PATCH}
+    n, npch = len(a["x"]), len(p["x"])
+    rv = int(ip[7])
+    soc = np.zeros((n, rv), np.float64)
+    fp = np.ascontiguousarray(fp, np.float64)
+    ip = np.ascontiguousarray(ip, np.int32)
+    uni = None if uniforms is None else np.ascontiguousarray(uniforms, np.float64)
+    ptr = lambda arr: arr.ctypes.data_as(ctypes.c_void_p)
+    failed = lib().orc_forage_step(
+        n, *[ptr(a[k]) for k, _ in _FORAGER], npch, *[ptr(p[k]) for k, _ in _PATCH],
+        ptr(fp), ptr(ip), ctypes.c_uint64(int(seed) & 0xFFFFFFFFFFFFFFFF),
+        None if uni is None else ptr(uni), ptr(soc))
+    return a, p, soc, int(failed)
+
+
+def philox4x32(ctr, key):
+    """The oracle's Philox-4x32-10 block (four uint32 words)."""
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    out = (ctypes.c_uint32 * 4)()
+    lib().orc_philox4x32(c, k, out)
+    return [int(v) for v in out]

@@ -680,3 +680,289 @@ void orc_social_vpf(int i, int n, const double *x, const double *y, const double
                                n_obs, xy, n_ex, visual_exclusion, out);
     free(inr); free(expl); free(nonx); free(xy);
 }
+
+/* ---------------------------------------------------------------- foraging step
+ *
+ * One step of the foraging simulation (abm/simulation/sims.py:734-858 without agent-agent
+ * collisions; Agent.update, abm/agent/agent.py:213-283), agents updated from one snapshot.
+ * Positions, orientation and speed are stored as float32 where the GPU step stores them, so
+ * the two can be compared exactly; decision variables, collected units and patches are FP64.
+ * Random draws: Philox-4x32-10 (Salmon et al., SC 2011) with the GPU step's counters, or the
+ * injected uniforms of the random walk.
+ *
+ * FP[30]: T_w Eps_w g_w B_w w_max T_u Eps_u g_u B_u u_max S_wu S_uw F_N F_R exp_vel_max
+ *         exp_theta_min exp_theta_max reloc_theta_max exp_stop_ratio width height window_pad
+ *         agent_radius consumption min_resc_quality max_resc_quality patch_radius fov0 fov1
+ *         vision_range
+ * IP[10]: Tau pooling_time teleport_exploit regenerate_patches allow_border_patch_overlap
+ *         min_resc_units max_resc_units rv visual_exclusion patchwise_exclusion
+ */
+enum { M_EXPLORE = 0, M_RELOCATE = 1, M_EXPLOIT = 2, M_POOL = 3, M_COLLIDE = 4, M_NONE = -1 };
+
+void orc_philox4x32(const uint32_t c_in[4], const uint32_t k_in[2], uint32_t out[4])
+{
+    uint32_t c0 = c_in[0], c1 = c_in[1], c2 = c_in[2], c3 = c_in[3];
+    uint32_t k0 = k_in[0], k1 = k_in[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static double orc_u01(uint32_t a, uint32_t b)
+{
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+static void orc_draw(uint64_t seed, uint32_t who, uint64_t count, uint32_t tag, uint32_t out[4])
+{
+    uint32_t c[4] = {who, (uint32_t)count, (uint32_t)(count >> 32), tag};
+    uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    orc_philox4x32(c, k, out);
+}
+
+typedef struct {
+    float *x, *y, *th, *v;
+    double *w, *u, *col, *colb;
+    int *mode, *ovr, *env, *envb, *pool, *patch;
+    uint32_t *nov;
+    uint64_t *draws;
+} ForagerArrays;
+
+static int f_get_mode(const ForagerArrays *a, const double *FP, int i)
+{
+    if (a->ovr[i] != M_NONE) return a->ovr[i];
+    return a->w[i] > FP[0] ? M_RELOCATE : M_EXPLORE;
+}
+
+/* notify_agent (sims.py:29-42) */
+static void f_notify(ForagerArrays *a, int Tau, int i, int status, int res_id)
+{
+    int before = a->env[i];
+    a->envb[i] = before;
+    a->env[i] = status;
+    uint32_t mask = Tau >= 32 ? 0xFFFFFFFFu : ((1u << Tau) - 1u);
+    a->nov[i] = ((a->nov[i] << 1) & mask) | ((status - before) > 0 ? 1u : 0u);
+    a->pool[i] = 1;
+    a->patch[i] = res_id;
+}
+
+static int f_pooling_done(const ForagerArrays *a, const int *IP, int i, int m)
+{
+    return ((m == M_POOL || m == M_RELOCATE) && a->pool[i]) || IP[1] == 0;
+}
+
+static double f_prove_orientation(double t)
+{
+    if (t < 0) t = 2 * ORC_PI + t;
+    if (t > ORC_PI * 2) t = t - 2 * ORC_PI;
+    return t;
+}
+
+/* add_new_resource_patch (sims.py:332-374) for slot k; returns 0 when no place was found */
+static int f_regenerate(int k, int np, double *px, double *py, double *pr, double *pu,
+                        double *pl, double *pq, const int *pid, uint64_t *pdraws,
+                        const double *FP, const int *IP, uint64_t seed)
+{
+    double r = FP[26], pad = FP[21], lox, hix, loy, hiy;
+    if (IP[4]) { lox = pad - r; hix = FP[19] + pad - r; loy = pad - r; hiy = FP[20] + pad - r; }
+    else { lox = pad; hix = FP[19] + pad - 2 * r; loy = pad; hiy = FP[20] + pad - 2 * r; }
+    uint64_t cnt = pdraws[k];
+    for (int tries = 0; tries <= 10000; ++tries) {
+        uint32_t w[4];
+        orc_draw(seed, (uint32_t)k, cnt++, 0x50415443u, w);
+        double x = lox + floor(orc_u01(w[0], w[1]) * (hix - lox));
+        double y = loy + floor(orc_u01(w[2], w[3]) * (hiy - loy));
+        int clear = 1;
+        for (int q = 0; q < np && clear; ++q) {
+            if (q == k || pid[q] < 0) continue;
+            double dx = (x + r) - (px[q] + pr[q]), dy = (y + r) - (py[q] + pr[q]);
+            double rr = r + pr[q];
+            clear = dx * dx + dy * dy >= rr * rr;
+        }
+        if (!clear) continue;
+        orc_draw(seed, (uint32_t)k, cnt++, 0x50415443u, w);
+        int span = IP[6] - IP[5];
+        double units = span > 0 ? (double)(IP[5] + (int)floor(orc_u01(w[0], w[1]) * span))
+                                : (double)IP[5];
+        px[k] = x; py[k] = y; pr[k] = r; pu[k] = units; pl[k] = units;
+        pq[k] = FP[24] + orc_u01(w[2], w[3]) * (FP[25] - FP[24]);
+        pdraws[k] = cnt;
+        return 1;
+    }
+    pdraws[k] = cnt;
+    return 0;
+}
+
+int orc_forage_step(int n, float *x, float *y, float *th, float *v, double *w, double *u,
+                    double *col, double *colb, int *mode, int *ovr, int *env, int *envb,
+                    int *pool, int *patch, uint32_t *nov, uint64_t *draws, int np, double *px,
+                    double *py, double *pr, double *pu, double *pl, double *pq, int *pid,
+                    uint64_t *pdraws, const double *FP, const int *IP, uint64_t seed,
+                    const double *uniforms, double *soc_out)
+{
+    ForagerArrays A = {x, y, th, v, w, u, col, colb, mode, ovr, env, envb, pool, patch, nov, draws};
+    const int Tau = IP[0], Rv = IP[7];
+    const double R = FP[22];
+    int failed = 0;
+    int *patch_of = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *destroyed = (int *)calloc((size_t)(np > 0 ? np : 1), sizeof(int));
+    /* 1. agent-resource interaction (sims.py:789-846) */
+    for (int i = 0; i < n; ++i) {
+        double cx = (double)x[i] + R, cy = (double)y[i] + R;
+        patch_of[i] = -1;
+        for (int k = 0; k < np && patch_of[i] < 0; ++k) {
+            if (pid[k] < 0) continue;
+            double dx = (px[k] + pr[k]) - cx, dy = (py[k] + pr[k]) - cy;
+            if (sqrt(dx * dx + dy * dy) < pr[k]) patch_of[i] = k;
+        }
+    }
+    for (int k = 0; k < np; ++k) {
+        if (pid[k] < 0) continue;
+        double pcx = px[k] + pr[k], pcy = py[k] + pr[k];
+        int destroy = 0;
+        for (int i = 0; i < n; ++i) {
+            if (patch_of[i] != k) continue;
+            double dx = pcx - ((double)x[i] + R), dy = pcy - ((double)y[i] + R);
+            double cl = fmod(atan2(dy, dx) + (double)th[i], 2.0 * ORC_PI);
+            if (cl < 0) cl += 2.0 * ORC_PI;
+            th[i] = (float)((double)th[i] + (cl - ORC_PI) * 0.02);
+            if (destroy) { f_notify(&A, Tau, i, -1, -1); continue; }
+            if (f_pooling_done(&A, IP, i, f_get_mode(&A, FP, i))) {
+                f_notify(&A, Tau, i, 1, pid[k]);
+                if (IP[2]) {
+                    x[i] = (float)(px[k] + pr[k] - R);
+                    y[i] = (float)(py[k] + pr[k] - R);
+                }
+            }
+            if (f_get_mode(&A, FP, i) == M_EXPLOIT) {
+                double want = FP[23], got;
+                if (want > pq[k]) want = pq[k];
+                if (pl[k] >= want) { pl[k] -= want; got = want; }
+                else { got = pl[k]; pl[k] = 0.0; }
+                colb[i] = col[i];
+                col[i] += got;
+                if (!(pl[k] > 0.0)) {
+                    destroy = 1;
+                    for (int j = 0; j < n; ++j) if (patch_of[j] == k) f_notify(&A, Tau, j, -1, -1);
+                }
+            }
+        }
+        destroyed[k] = destroy;
+    }
+    for (int k = 0; k < np; ++k) {
+        if (!destroyed[k]) continue;
+        if (!IP[3] || !f_regenerate(k, np, px, py, pr, pu, pl, pq, pid, pdraws, FP, IP, seed)) {
+            if (IP[3]) failed++;
+            pid[k] = -1;
+        }
+    }
+    int *exploit = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; ++i) {
+        if (patch_of[i] < 0) {
+            int m = f_get_mode(&A, FP, i);
+            if (f_pooling_done(&A, IP, i, m) || m == M_EXPLOIT) f_notify(&A, Tau, i, -1, -1);
+        }
+        exploit[i] = ovr[i] == M_EXPLOIT;
+    }
+    /* 2. social fields from the post-interaction snapshot (Agent.calc_social_V_proj) */
+    double *xd = (double *)malloc(sizeof(double) * 4 * (size_t)(n > 0 ? n : 1));
+    double *yd = xd + n, *rd = xd + 2 * (size_t)n, *td = xd + 3 * (size_t)n;
+    for (int i = 0; i < n; ++i) { xd[i] = x[i]; yd[i] = y[i]; rd[i] = R; td[i] = th[i]; }
+    for (int i = 0; i < n; ++i)
+        orc_social_vpf(i, n, xd, yd, rd, td, exploit, patch, FP[29], IP[8], IP[9], Rv, FP[27],
+                       FP[28], soc_out + (size_t)i * Rv);
+    /* 3. agent update (agent.py:213-283) */
+    for (int i = 0; i < n; ++i) {
+        const double *V = soc_out + (size_t)i * Rv;
+        int half = Rv / 2;
+        double total = 0, left = 0;
+        for (int k = 0; k < Rv; ++k) { total += V[k]; if (k < half) left += V[k]; }
+        double I_priv = FP[12] * (nov[i] ? 1.0 : 0.0) + FP[13] * (col[i] - colb[i]);
+        double wv = w[i], uv = u[i];
+        double w_p = wv > FP[0] ? wv : 0.0, u_p = uv > FP[5] ? uv : 0.0;
+        double dw = FP[1] * (total / Rv) - FP[2] * (wv - FP[3]) - u_p * FP[11];
+        double du = FP[6] * I_priv - FP[7] * (uv - FP[8]) - w_p * FP[10];
+        wv += dw; uv += du;
+        if (wv > FP[4]) wv = FP[4];
+        if (wv < -FP[4]) wv = -FP[4];
+        if (uv > FP[9]) uv = FP[9];
+        if (uv < -FP[9]) uv = -FP[9];
+        w[i] = wv; u[i] = uv;
+        int o = ovr[i], md = mode[i];
+        double vel0 = (double)v[i], vel = 0.0, theta = 0.0;
+        int cur = o != M_NONE ? o : (wv > FP[0] ? M_RELOCATE : M_EXPLORE);
+        if (cur != M_COLLIDE) {
+            int tw = wv > FP[0], tu = uv > FP[0], on = env[i] == 1, act;
+            if (!tw && !tu) act = 0;
+            else if (tw && tu) act = on ? 2 : 1;
+            else if (tw) act = 1;
+            else act = on ? 2 : 0;
+            if (act == 0) {
+                double r01;
+                if (uniforms) r01 = uniforms[i];
+                else {
+                    uint32_t wd[4];
+                    orc_draw(seed, (uint32_t)i, draws[i], 0x57414C4Bu, wd);
+                    r01 = orc_u01(wd[0], wd[1]);
+                    draws[i] += 1;
+                }
+                vel = FP[14];
+                theta = FP[15] + (FP[16] - FP[15]) * r01;
+                md = M_EXPLORE; o = M_NONE;
+            } else if (act == 1) {
+                double le = left / half, re = (total - left) / (Rv - half);
+                vel = FP[14] - vel0;
+                theta = (le - re) * FP[17];
+                md = M_RELOCATE; o = M_NONE;
+            } else {
+                vel = -vel0 * FP[18];
+                theta = 0.0;
+                md = M_EXPLOIT; o = M_EXPLOIT;
+            }
+        }
+        mode[i] = md; ovr[i] = o;
+        double t = f_prove_orientation((double)th[i] + theta);
+        double vv = vel0 + vel;
+        int after = o != M_NONE ? o : (wv > FP[0] ? M_RELOCATE : M_EXPLORE);
+        if (after == M_EXPLORE && fabs(vv) > 1.0) vv = FP[14];
+        double xx = (double)x[i] + vv * cos(t), yy = (double)y[i] - vv * sin(t);
+        double bx0 = FP[21], bx1 = FP[21] + FP[19], by0 = FP[21], by1 = FP[21] + FP[20];
+        double cx = xx + R, cy = yy + R;
+        if (cx < bx0) {
+            xx = bx0 - R;
+            if (ORC_PI / 2 <= t && t < ORC_PI) t -= ORC_PI / 2;
+            else if (ORC_PI <= t && t <= 3 * ORC_PI / 2) t += ORC_PI / 2;
+            t = f_prove_orientation(t);
+        }
+        if (cx > bx1) {
+            xx = bx1 - R - 1;
+            if (3 * ORC_PI / 2 <= t && t < 2 * ORC_PI) t -= ORC_PI / 2;
+            else if (0 <= t && t <= ORC_PI / 2) t += ORC_PI / 2;
+            t = f_prove_orientation(t);
+        }
+        if (cy < by0) {
+            yy = by0 - R;
+            if (ORC_PI / 2 <= t && t <= ORC_PI) t += ORC_PI / 2;
+            else if (0 <= t && t < ORC_PI / 2) t -= ORC_PI / 2;
+            t = f_prove_orientation(t);
+        }
+        if (cy > by1) {
+            yy = by1 - R - 1;
+            if (3 * ORC_PI / 2 <= t && t <= 2 * ORC_PI) t += ORC_PI / 2;
+            else if (ORC_PI <= t && t < 3 * ORC_PI / 2) t -= ORC_PI / 2;
+            t = f_prove_orientation(t);
+        }
+        x[i] = (float)xx; y[i] = (float)yy; th[i] = (float)t; v[i] = (float)vv;
+        colb[i] = col[i];
+    }
+    free(patch_of); free(destroyed); free(exploit); free(xd);
+    return failed;
+}

@@ -1,6 +1,6 @@
 """CPU-only checks of the C-ABI library: it loads, exports every entry point declared in
-include/abm_vpf.h, and its host-side logic (numpy-exact grids, defaults, argument
-validation) is right.  No call here reaches a CUDA kernel."""
+include/*.h, and its host-side logic (numpy-exact grids, defaults, argument validation) is
+right.  No call here reaches a CUDA kernel."""
 import ctypes
 import math
 import os
@@ -19,9 +19,14 @@ def lib():
 
 
 def declared_functions():
-    src = open(os.path.join(ROOT, "include", "abm_vpf.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(abm_[a-z0-9_]+)\s*\(", src)))
+    names = set()
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(abm_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
 
 
 def test_exports_every_declared_symbol(lib):
