@@ -15,6 +15,7 @@
 // numbers come from a Philox-4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
 // "Parallel random numbers: as easy as 1, 2, 3", SC 2011) keyed by the seed, with one counter
 // per agent and per patch slot, so a step is reproducible and graph-replayable.
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -105,57 +106,82 @@ __device__ inline bool pooling_done(const ForageArgs &a, int i, int m) {
            a.p.pooling_time == 0;
 }
 
-// Rescource.deplete (rescource.py:118-133); returns the units taken, sets *empty.
-__device__ inline double deplete(const ForageArgs &a, int k, double want, bool *empty) {
-    if (want > a.pt.quality[k]) want = a.pt.quality[k];
-    double got;
-    if (a.pt.left[k] >= want) {
-        a.pt.left[k] -= want;
-        got = want;
-    } else {
-        got = a.pt.left[k];
-        a.pt.left[k] = 0.0;
-    }
-    *empty = !(a.pt.left[k] > 0.0);
-    return got;
-}
-
-// Sequential agent loop of one patch (sims.py:800-838), run by one thread.
+// Agent loop of one patch (sims.py:800-838), run by one warp.  Its members are the agents whose
+// centre is inside the patch, in agent order.  Each member only touches its own state, except
+// through the patch's stock: every exploiting member takes want = min(consumption, quality)
+// in turn, and the first whose take leaves nothing (!(left > 0)) empties the patch; call it D.
+// So the loop reduces to (1) lane 0 replaying the stock's subtractions over the exploiting
+// members to find D, then (2) every member applying its own sequence in parallel:
+//   before D: [pooling notify(1, id) + teleport] [take want] [notify(-1): D's notify-all]
+//   D:        [pooling notify(1, id) + teleport] [take the rest] [notify(-1)]
+//   after D:  [notify(-1): D's notify-all] [notify(-1): the destroy branch]
+// (without D, members just take their pooling notification and their want).  The turn
+// towards the patch centre reads only the agent's own position and orientation and comes
+// first for every member.
 __device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed) {
+    const int lane = threadIdx.x & 31;
     const double R = a.p.agent_radius;
     const double pcx = a.pt.x[k] + a.pt.radius[k], pcy = a.pt.y[k] + a.pt.radius[k];
-    bool destroy = false;
-    for (int i = 0; i < a.n; ++i) {
-        if (a.patch_of[i] != k) continue;
+    const double want = a.p.consumption > a.pt.quality[k] ? a.pt.quality[k] : a.p.consumption;
+    double left = a.pt.left[k];
+    int D = INT_MAX;       // agent index of the member that empties the patch
+    double take_D = 0.0;
+    // (1) the stock, in member order
+    for (int base = 0; base < a.n && D == INT_MAX; base += 32) {
+        const int j = base + lane;
+        const bool member = j < a.n && a.patch_of[j] == k;
+        const unsigned ex = __ballot_sync(ABM_FULL_MASK, member && get_mode(a, j) == ABM_MODE_EXPLOIT);
+        if (lane == 0) {
+            for (unsigned m = ex; m; m &= m - 1u) {   // Rescource.deplete, rescource.py:118-133
+                double got;
+                if (left >= want) {
+                    left -= want;
+                    got = want;
+                } else {
+                    got = left;
+                    left = 0.0;
+                }
+                if (!(left > 0.0)) {
+                    D = base + __ffs(m) - 1;
+                    take_D = got;
+                    break;
+                }
+            }
+        }
+        D = __shfl_sync(ABM_FULL_MASK, D, 0);
+    }
+    take_D = __shfl_sync(ABM_FULL_MASK, take_D, 0);
+    left = __shfl_sync(ABM_FULL_MASK, left, 0);
+    // (2) every member's own sequence
+    for (int base = 0; base < a.n; base += 32) {
+        const int i = base + lane;
+        if (!(i < a.n && a.patch_of[i] == k)) continue;
         // bias_agent_towards_res_center (sims.py:544-552)
         const double dx = pcx - ((double)a.ag.x[i] + R), dy = pcy - ((double)a.ag.y[i] + R);
         double cl = fmod(atan2(dy, dx) + (double)a.ag.theta[i], 2.0 * M_PI);
         if (cl < 0) cl += 2.0 * M_PI;   // Python's % with a positive divisor
         a.ag.theta[i] = (float)((double)a.ag.theta[i] + (cl - M_PI) * 0.02);
-        if (destroy) {
+        if (i > D) {
+            notify(a, i, -1, -1);
             notify(a, i, -1, -1);
             continue;
         }
-        if (pooling_done(a, i, get_mode(a, i))) {
+        const int mode = get_mode(a, i);
+        if (pooling_done(a, i, mode)) {
             notify(a, i, 1, a.pt.id[k]);
             if (a.p.teleport_exploit) {
                 a.ag.x[i] = (float)(a.pt.x[k] + a.pt.radius[k] - R);
                 a.ag.y[i] = (float)(a.pt.y[k] + a.pt.radius[k] - R);
             }
         }
-        if (get_mode(a, i) == ABM_MODE_EXPLOIT) {
-            bool empty = false;
-            const double got = deplete(a, k, a.p.consumption, &empty);
+        if (mode == ABM_MODE_EXPLOIT) {
             a.ag.collected_before[i] = a.ag.collected[i];
-            a.ag.collected[i] += got;
-            if (empty) {
-                destroy = true;
-                for (int j = 0; j < a.n; ++j)
-                    if (a.patch_of[j] == k) notify(a, j, -1, -1);
-            }
+            a.ag.collected[i] += i == D ? take_D : want;
         }
+        if (D != INT_MAX) notify(a, i, -1, -1);
     }
-    *destroyed = destroy;
+    if (lane == 0) a.pt.left[k] = left;
+    *destroyed = D != INT_MAX;
 }
 
 // add_new_resource_patch (sims.py:332-374) for slot k, with the slot's random stream: uniform
@@ -218,6 +244,16 @@ __global__ void __launch_bounds__(kResourceThreads) forage_resource_kernel(Forag
         int hit = -1;
         for (int k = 0; k < a.np && hit < 0; ++k) {
             if (a.pt.id[k] < 0) continue;   // a slot whose regeneration failed
+            // FP32 screen (error far below the one-pixel margin), FP64 test near the edge
+            const float rk = (float)a.pt.radius[k];
+            const float fx = (float)(a.pt.x[k] + a.pt.radius[k]) - (float)cx;
+            const float fy = (float)(a.pt.y[k] + a.pt.radius[k]) - (float)cy;
+            const float f2 = fx * fx + fy * fy;
+            if (f2 > (rk + 1.f) * (rk + 1.f)) continue;
+            if (f2 < (rk - 1.f) * (rk - 1.f) && rk > 1.f) {
+                hit = k;
+                continue;
+            }
             const double dx = (a.pt.x[k] + a.pt.radius[k]) - cx;
             const double dy = (a.pt.y[k] + a.pt.radius[k]) - cy;
             if (sqrt(dx * dx + dy * dy) < a.pt.radius[k]) hit = k;
@@ -226,13 +262,12 @@ __global__ void __launch_bounds__(kResourceThreads) forage_resource_kernel(Forag
     }
     for (int k = tid; k < a.np; k += blockDim.x) destroyed[k] = 0;
     __syncthreads();
-    // 2. each patch's agents in agent order (one lane per patch: the loop is sequential)
+    // 2. each patch's agents in agent order (one warp per patch: the loop is sequential)
     for (int k = warp; k < a.np; k += nw) {
-        if (lane == 0 && a.pt.id[k] >= 0) {
-            bool d = false;
-            patch_loop(a, k, &d);
-            destroyed[k] = d ? 1 : 0;
-        }
+        if (a.pt.id[k] < 0) continue;   // warp-uniform
+        bool d = false;
+        patch_loop(a, k, &d);
+        if (lane == 0) destroyed[k] = d ? 1 : 0;
     }
     __syncthreads();
     // 3. emptied patches are killed and regenerated in patch order (kill_resource)
@@ -266,21 +301,29 @@ __device__ inline double prove_orientation(double t) {
     return t;
 }
 
-__global__ void __launch_bounds__(128) forage_update_kernel(ForageArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
+constexpr int kUpdateWarps = 4;
+
+// One warp per agent: the lanes count the social field's pixels (coalesced word loads), lane 0
+// applies the update.
+__global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(ForageArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kUpdateWarps + (threadIdx.x >> 5);
+    if (i >= a.n) return;   // warp-uniform
     const abm_forage_params &p = a.p;
     // social field statistics: mean, and the left / right halves of F_reloc_LR
     const uint32_t *bits = a.soc + (size_t)i * a.words;
     const int rv = p.rv, half = rv / 2;
     int total = 0, left = 0;
-    for (int wd = 0; wd < a.words; ++wd) {
+    for (int wd = lane; wd < a.words; wd += 32) {
         const uint32_t b = bits[wd];
         total += __popc(b);
         const int lo = wd * 32;
         if (lo + 32 <= half) left += __popc(b);
         else if (lo < half) left += __popc(b & ((1u << (half - lo)) - 1u));
     }
+    total = __reduce_add_sync(ABM_FULL_MASK, total);
+    left = __reduce_add_sync(ABM_FULL_MASK, left);
+    if (lane != 0) return;
     // calc_I_priv (agent.py:180-187): novelty memory and the units collected this step
     const double I_priv = p.F_N * (a.ag.novelty[i] ? 1.0 : 0.0) +
                           p.F_R * (a.ag.collected[i] - a.ag.collected_before[i]);
@@ -345,8 +388,10 @@ __global__ void __launch_bounds__(128) forage_update_kernel(ForageArgs a) {
     double v = vel0 + vel;
     const int after = ovr != ABM_MODE_NONE ? ovr : (w > p.T_w ? ABM_MODE_RELOCATE : ABM_MODE_EXPLORE);
     if (after == ABM_MODE_EXPLORE && fabs(v) > 1.0) v = p.exp_vel_max;
-    double x = (double)a.ag.x[i] + v * cos(th);
-    double y = (double)a.ag.y[i] - v * sin(th);
+    double sn, cs;
+    sincos(th, &sn, &cs);
+    double x = (double)a.ag.x[i] + v * cs;
+    double y = (double)a.ag.y[i] - v * sn;
     const double R = p.agent_radius, bx0 = p.window_pad, bx1 = p.window_pad + p.width;
     const double by0 = p.window_pad, by1 = p.window_pad + p.height;
     const double cx = x + R, cy = y + R;
@@ -465,7 +510,7 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
                                p->visual_exclusion, p->patchwise_exclusion, p->rv, p->fov0,
                                p->fov1, soc_bits_dev, diag_dev, stream);
     if (st < 0) return st;
-    forage_update_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+    forage_update_kernel<<<(n + kUpdateWarps - 1) / kUpdateWarps, 32 * kUpdateWarps, 0, s>>>(a);
     return check_cuda(cudaGetLastError(), "forage_update_kernel launch");
 }
 

@@ -76,9 +76,13 @@ static __host__ __device__ __forceinline__ SocialSmem social_smem(int words, int
 
 static size_t social_smem_bytes(int words, int cap) { return social_smem(words, cap).total; }
 
-__global__ void __launch_bounds__(32) vpf_social_kernel(const SocialArgs a) {
+constexpr int kSocialWarps = 4;
+
+__global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const SocialArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int lane = threadIdx.x;
+    __shared__ int s_count, s_over;
+    __shared__ unsigned s_resolved, s_near;
+    const int tid = threadIdx.x, lane = tid & 31, nthr = blockDim.x;
     const int i = blockIdx.x;
     const int words = a.g.words, rv = a.g.rv, cap = a.cap;
     const SocialSmem L = social_smem(words, cap);
@@ -86,7 +90,13 @@ __global__ void __launch_bounds__(32) vpf_social_kernel(const SocialArgs a) {
     SocialEntry *ent = reinterpret_cast<SocialEntry *>(smem + L.ent);
     int *sidx = reinterpret_cast<int *>(smem + L.sidx);     // entries by ascending distance
     int2 *trim = reinterpret_cast<int2 *>(smem + L.trim);   // trimmed (start, end) per entry
-    for (int w = lane; w < words; w += 32) vb[w] = 0u;
+    for (int w = tid; w < words; w += nthr) vb[w] = 0u;
+    if (tid == 0) {
+        s_count = 0;
+        s_over = 0;
+        s_resolved = 0;
+        s_near = 0;
+    }
 
     const float xi = a.x[i], yi = a.y[i];
     const float ri = a.radius ? a.radius[i] : a.radius0;
@@ -101,13 +111,13 @@ __global__ void __launch_bounds__(32) vpf_social_kernel(const SocialArgs a) {
     f.s = f.sd.hi + f.sd.lo;
     const float band = 4e-6f;   // FP32 bearing error bound (1e-6 rad) with margin
     unsigned resolved = 0, nearc = 0;
-    __syncwarp();
+    __syncthreads();
 
-    // ---- obstacles: in vision range, classified, inside the FOV
-    int m = 0;   // warp-uniform entry count
+    // ---- obstacles: in vision range, classified, inside the FOV (one candidate per thread;
+    // the entries' storage order is free: the rank below orders them)
     bool overflow = false;
-    for (int jb = 0; jb < a.n; jb += 32) {
-        const int j = jb + lane;
+    for (int jb = 0; jb < a.n; jb += nthr) {
+        const int j = jb + tid;
         bool keep = false;
         SocialEntry e;
         if (j < a.n) {
@@ -183,31 +193,37 @@ __global__ void __launch_bounds__(32) vpf_social_kernel(const SocialArgs a) {
             }
         }
         const unsigned km = __ballot_sync(ABM_FULL_MASK, keep);
-        const int pos = m + __popc(km & ((1u << lane) - 1u));
+        int base = 0;
+        if (lane == 0 && km) base = atomicAdd(&s_count, __popc(km));
+        base = __shfl_sync(ABM_FULL_MASK, base, 0);
+        const int pos = base + __popc(km & ((1u << lane) - 1u));
         if (keep) {
             if (pos < cap) ent[pos] = e;
             else overflow = true;
         }
-        m += __popc(km);
     }
-    const bool over = __any_sync(ABM_FULL_MASK, overflow);
-    __syncwarp();
-    if (over) m = 0;   // more obstacles than the capacity: reported, field left empty
+    if (__any_sync(ABM_FULL_MASK, overflow) && lane == 0) s_over = 1;
+    __syncthreads();
+    const bool over = s_over != 0;
+    int m = over ? 0 : s_count;   // more obstacles than the capacity: reported, field empty
 
-    // ---- stable ascending rank by exact squared distance (ties keep the list order)
-    for (int e = lane; e < m; e += 32) {
-        const SocialEntry me = ent[e];
+    // ---- stable ascending rank by exact squared distance (ties keep the list order): one
+    // entry per thread, every other entry read at the same address by the whole block
+    for (int e = tid; e < m; e += nthr) {
+        const float kh = ent[e].dkh, kl = ent[e].dkl;
+        const int ko = ent[e].ord;
         int rank = 0;
         for (int q = 0; q < m; ++q) {
-            const SocialEntry o = ent[q];
-            rank += (o.dkh < me.dkh) || (o.dkh == me.dkh && o.dkl < me.dkl) ||
-                    (o.dkh == me.dkh && o.dkl == me.dkl && o.ord < me.ord);
+            const float oh = ent[q].dkh, ol = ent[q].dkl;
+            const int oo = ent[q].ord;
+            rank += (oh < kh) || (oh == kh && ol < kl) || (oh == kh && ol == kl && oo < ko);
         }
         sidx[rank] = e;
     }
-    __syncwarp();
-    // ---- trim each interval against the strictly closer ones, in ascending order
-    for (int r = lane; r < m; r += 32) {
+    __syncthreads();
+    // ---- trim each interval against the strictly closer ones, in ascending order (one
+    // focal interval per thread)
+    for (int r = tid; r < m; r += nthr) {
         const int fe = sidx[r];
         const SocialEntry F = ent[fe];
         int sx = F.s0, ex = F.e0;
@@ -225,9 +241,9 @@ __global__ void __launch_bounds__(32) vpf_social_kernel(const SocialArgs a) {
         }
         trim[fe] = make_int2(sx, ex);
     }
-    __syncwarp();
+    __syncthreads();
     // ---- fill the surviving social intervals (agent.py:576-588)
-    for (int e = lane; e < m; e += 32) {
+    for (int e = tid; e < m; e += nthr) {
         if (!ent[e].social) continue;
         int s = trim[e].x, en = trim[e].y;
         if (s < 0) {
@@ -240,11 +256,11 @@ __global__ void __launch_bounds__(32) vpf_social_kernel(const SocialArgs a) {
         }
         np_slice_fill(vb, rv, s, en);
     }
-    __syncwarp();
+    __syncthreads();
     // ---- flip and FOV mask (agent.py:591-595): out[k] = raw[rv - 1 - k], 0 outside the FOV
     const int shift = words * 32 - rv;
     uint32_t *dst = a.out + (size_t)i * words;
-    for (int w = lane; w < words; w += 32) {
+    for (int w = tid; w < words; w += nthr) {
         const uint32_t lo = __brev(vb[words - 1 - w]);
         const uint32_t hi = (w + 1 < words) ? __brev(vb[words - 2 - w]) : 0u;
         uint32_t word = shift ? __funnelshift_r(lo, hi, shift) : lo;
@@ -257,9 +273,14 @@ __global__ void __launch_bounds__(32) vpf_social_kernel(const SocialArgs a) {
     }
     const unsigned tr = __reduce_add_sync(ABM_FULL_MASK, resolved);
     const unsigned tn = __reduce_add_sync(ABM_FULL_MASK, nearc);
-    if (a.diag && lane == 0) {
-        if (tr) atomicAdd(&a.diag[ABM_DIAG_PAIRS_RESOLVED], (unsigned long long)tr);
-        if (tn) atomicAdd(&a.diag[ABM_DIAG_NEAR_BOUNDARY], (unsigned long long)tn);
+    if (lane == 0 && (tr || tn)) {
+        atomicAdd(&s_resolved, tr);
+        atomicAdd(&s_near, tn);
+    }
+    __syncthreads();
+    if (a.diag && tid == 0) {
+        if (s_resolved) atomicAdd(&a.diag[ABM_DIAG_PAIRS_RESOLVED], (unsigned long long)s_resolved);
+        if (s_near) atomicAdd(&a.diag[ABM_DIAG_NEAR_BOUNDARY], (unsigned long long)s_near);
         if (over) atomicAdd(&a.diag[ABM_DIAG_CAPACITY], 1ull);
     }
 }
@@ -339,6 +360,6 @@ extern "C" int abm_vpf_social_fields(const float *x_dev, const float *y_dev,
                              200 * 1024);
         attr = true;
     }
-    vpf_social_kernel<<<n, 32, smem, (cudaStream_t)stream>>>(a);
+    vpf_social_kernel<<<n, 32 * kSocialWarps, smem, (cudaStream_t)stream>>>(a);
     return check_cuda(cudaGetLastError(), "vpf_social_kernel launch");
 }

@@ -147,6 +147,11 @@ class ForageParams:
                 visual_exclusion=bool(i("VISUAL_EXCLUSION", d.visual_exclusion)),
                 patchwise_exclusion=bool(i("PATCHWISE_SOCIAL_EXCLUSION",
                                            d.patchwise_exclusion)))
+        # sims.py:176-179: a negative maximum means a constant (units: randint(min, min + 1))
+        if p.max_resc_quality < 0:
+            p.max_resc_quality = p.min_resc_quality
+        if p.max_resc_units < 0:
+            p.max_resc_units = p.min_resc_units + 1
         return dataclasses.replace(p, **over)
 
 

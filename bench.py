@@ -331,6 +331,64 @@ def batched_leg(torch, lib, stream, steps=BATCHED["steps"], flush=None):
             "autotune": {"best": tuned["best"], "table": compact_table(tuned["tried"])}}
 
 
+# ---------------------------------------------------------------------- foraging leg
+FORAGE = dict(workload="collective_foraging", n_agents=100, radius=10.0, arena=[1000.0, 1000.0],
+              n_patches=3, patch_radius=30.0, patch_units=1000, quality=1.0, consumption=1.0,
+              rv=1200, agent_fov=0.5, vision_range=2000.0, visual_exclusion=True,
+              teleport=False, pooling_time=0, steps=10000, graph_chunk=100, seed=5,
+              step="resource interaction + social VPF + decision/motion update (3 launches)")
+
+
+def forage_params():
+    from abm_gb300.foraging import ForageParams
+    return ForageParams(width=1000.0, height=1000.0, agent_radius=10.0, patch_radius=30.0,
+                        min_resc_units=1000, max_resc_units=1001, min_resc_quality=1.0,
+                        max_resc_quality=1.0, consumption=1.0, rv=1200, fov=0.5,
+                        vision_range=2000.0, visual_exclusion=True, teleport_exploit=False,
+                        pooling_time=0, seed=FORAGE["seed"])
+
+
+def forage_leg(torch, steps=FORAGE["steps"], with_cpu=True):
+    """The foraging workload run for `steps` steps in CUDA graphs of 100 steps; foraging
+    efficiency (units per agent per step, data_loader.py:1333-1346) over the run; the oracle
+    step on the host for a bounded sample of steps."""
+    from abm_gb300.foraging import ForagingSim, efficiency
+    prm = forage_params()
+    sim = ForagingSim(prm, n_agents=FORAGE["n_agents"], n_patches=FORAGE["n_patches"],
+                      init_seed=FORAGE["seed"])
+    chunk = FORAGE["graph_chunk"]
+    sim.run(chunk, chunk=chunk)                     # capture + one warm-up replay
+    torch.cuda.synchronize()
+    c0, t0 = sim.collected(), sim.t
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sim.run(steps, chunk=chunk)
+    e1.record()
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    eff = efficiency(c0, sim.collected(), sim.t - t0)
+    n = FORAGE["n_agents"]
+    out = {"workload": FORAGE, "value": n * steps / t, "unit": METRIC,
+           "ms_per_step": t / steps * 1e3, "steps": steps, "gpu_launches": 3 * steps,
+           "efficiency_mean": float(eff.mean()), "efficiency_max": float(eff.max()),
+           "diagnostics": {"nonfinite": int(sim.diag[2].item()),
+                           "failed_regenerations": int(sim.diag[4].item())}}
+    if with_cpu:
+        import oracle
+        fp, ip, seed = prm.oracle_arrays()
+        ag, pt = sim.agents_numpy(), sim.patches_numpy()
+        k, t_cpu = 0, 0.0
+        while t_cpu < 10.0 and k < 400:
+            a = time.perf_counter()
+            ag, pt, _, _ = oracle.forage_step(ag, pt, fp, ip, seed)
+            t_cpu += time.perf_counter() - a
+            k += 1
+        out["cpu_baseline"] = {"value": n * k / t_cpu, "unit": METRIC, "cores": 1,
+                               "kind": "port", "sample": f"{k} steps of the same arena, FP64 C "
+                                                         "restatement, one thread"}
+    return out
+
+
 # ---------------------------------------------------------------------- differentiable leg
 ADJOINT = dict(workload="vf_differentiable", n_agents=256, radius=10.0, arena=[1500.0, 1500.0],
                steps=200, dt=0.1, checkpoint=20,
@@ -519,6 +577,8 @@ def run_gb300(args, rank, world):
         line["batched"] = batched_leg(torch, lib, stream, flush=flush)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_leg(torch)
+    if not args.no_forage:
+        line["forage"] = forage_leg(torch, with_cpu=not args.no_cpu_baseline)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(state)
     print(json.dumps(line), flush=True)
@@ -533,6 +593,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-forage", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -72,3 +72,23 @@ def test_forage_oracle_branches_covered():
     assert emptied >= 2
     notified = sum(int(np.sum(c["out_env_status"] == 1)) for c in cases)
     assert notified >= 5
+
+
+def test_forage_params_from_env_and_round_trip():
+    """.env keys of abm/app.py and the -1 maxima of sims.py:176-179; the oracle arrays and the
+    C struct carry the same values."""
+    import math
+    from abm_gb300.foraging import ForageParams
+    env = {"N": "10", "MIN_RESOURCE_PER_PATCH": "100", "MAX_RESOURCE_PER_PATCH": "-1",
+           "MIN_RESOURCE_QUALITY": "0.25", "MAX_RESOURCE_QUALITY": "-1", "AGENT_FOV": "0.5",
+           "VISION_RANGE": "2000", "POOLING_TIME": "0", "TELEPORT_TO_MIDDLE": "0",
+           "DEC_TW": "0.4", "MOV_REL_TH_MAX": "0.7", "VISUAL_FIELD_RESOLUTION": "320"}
+    p = ForageParams.from_env(env, seed=3)
+    assert (p.min_resc_units, p.max_resc_units) == (100, 101)
+    assert (p.min_resc_quality, p.max_resc_quality) == (0.25, 0.25)
+    assert p.T_w == 0.4 and p.reloc_theta_max == 0.7 and p.rv == 320 and not p.teleport_exploit
+    fp, ip, seed = p.oracle_arrays()
+    assert ForageParams.from_arrays(fp, ip, seed) == p
+    c = p.to_c()
+    assert c.fov0 == -0.5 * math.pi and c.fov1 == 0.5 * math.pi and c.seed == 3
+    assert c.min_resc_units == 100 and c.max_resc_units == 101 and c.T_w == 0.4
