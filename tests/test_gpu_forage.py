@@ -94,3 +94,30 @@ def test_forage_graph_replay_and_determinism():
     for k in pa:
         assert np.array_equal(pa[k], pb[k]), k
     assert a.collected().sum() > 0
+
+
+def test_forage_efficiency_ensemble_matches_reference():
+    """Long runs: the mean foraging efficiency (data_loader.py:1333-1346) of GPU runs (snapshot
+    updates, Philox draws) agrees with whole runs of the reference's own sequential loop
+    (tests/golden/make_forage_ensemble.py) from the same initial placements, within four
+    combined standard errors of the run means."""
+    import os
+    from conftest import GOLDEN
+    from abm_gb300.foraging import ForageParams, ForagingSim, efficiency, initial_state
+    z = np.load(os.path.join(GOLDEN, "forage_ensemble.npz"))
+    ref = z["eff"].mean(axis=1)                    # per run
+    T, T0 = int(z["T"]), int(z["T0"])
+    runs = []
+    for seed in z["seeds"]:
+        for rep in range(4):
+            prm = ForageParams.from_arrays(z["fp"], z["ip"], seed=int(seed) * 16 + rep)
+            ag, pt = initial_state(prm, int(z["n_agents"]), int(z["n_patches"]), seed=int(seed))
+            sim = ForagingSim(prm, agents=ag, patches=pt)
+            sim.run(T0, chunk=100)
+            c0 = sim.collected()
+            sim.run(T - T0, chunk=100)
+            runs.append(efficiency(c0, sim.collected(), T - T0).mean())
+    gpu = np.array(runs)
+    se = np.sqrt(gpu.var(ddof=1) / len(gpu) + ref.var(ddof=1) / len(ref))
+    assert abs(gpu.mean() - ref.mean()) <= 4 * se, (gpu.mean(), ref.mean(), se)
+    assert gpu.mean() > 0.01
