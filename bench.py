@@ -389,6 +389,38 @@ def forage_leg(torch, steps=FORAGE["steps"], with_cpu=True):
     return out
 
 
+# ---------------------------------------------------------------------- metarunner leg
+METARUNNER = dict(workload="metarunner_grid", criteria=["Tunable VF_ALP0 linspace(0.1, 3, 16)",
+                                                         "Tunable VF_BET0 linspace(0.1, 3, 32)",
+                                                         "Constant N 100"],
+                  num_batches=1, arena=[1000.0, 1000.0], rv=1200, radius=10.0, steps=1000,
+                  graph_chunk=100, seed=1)
+
+
+def metarunner_leg(torch):
+    """A metarunner sweep (the reference's MetaProtocol definitions) run end to end through
+    abm_gb300.metarunner.BatchedProtocol.run: expansion, initial states, batched launches in
+    graphs of 100 steps and the final states back on the host, timed by the wall clock."""
+    from abm_gb300 import metarunner as mr
+    base = {"ENV_WIDTH": "1000", "ENV_HEIGHT": "1000", "VISUAL_FIELD_RESOLUTION": "1200",
+            "RADIUS_AGENT": "10", "VF_ALP1": "0.08", "VF_BET1": "0.08"}
+    bp = mr.BatchedProtocol(base, num_batches=METARUNNER["num_batches"])
+    bp.add_criterion(mr.Tunable("VF_ALP0", 0.1, 3.0, 16))
+    bp.add_criterion(mr.Tunable("VF_BET0", 0.1, 3.0, 32))
+    bp.add_criterion(mr.Constant("N", 100))
+    steps = METARUNNER["steps"]
+    bp.run(steps // 10, seed=METARUNNER["seed"])   # warm-up (tables, workspace)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = bp.run(steps, seed=METARUNNER["seed"], chunk=METARUNNER["graph_chunk"])
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    agents = sum(len(r["x"]) for r in res)
+    return {"workload": METARUNNER, "configurations": len(res), "groups": len(bp.groups()),
+            "value": agents * steps / t, "unit": METRIC, "wall_s": t,
+            "timing": "wall clock of BatchedProtocol.run (setup, capture, launches, results)"}
+
+
 # ---------------------------------------------------------------------- differentiable leg
 ADJOINT = dict(workload="vf_differentiable", n_agents=256, radius=10.0, arena=[1500.0, 1500.0],
                steps=200, dt=0.1, checkpoint=20,
@@ -579,6 +611,8 @@ def run_gb300(args, rank, world):
         line["adjoint"] = adjoint_leg(torch)
     if not args.no_forage:
         line["forage"] = forage_leg(torch, with_cpu=not args.no_cpu_baseline)
+    if not args.no_batched:
+        line["metarunner"] = metarunner_leg(torch)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(state)
     print(json.dumps(line), flush=True)
