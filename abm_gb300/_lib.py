@@ -159,6 +159,9 @@ SIGNATURES = [
     ("abm_vpf_get_step_mode", c_int32, [c_i32_p, c_i32_p]),
     ("abm_vpf_set_step_split", c_int32, [c_int32]),
     ("abm_vpf_get_step_split", c_int32, [c_i32_p]),
+    ("abm_vpf_flock_step_host", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
+      ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), ctypes.c_void_p]),
     ("abm_forage_params_default", c_int32, [ctypes.POINTER(AbmForageParams)]),
     ("abm_forage_step", c_int32,
      [ctypes.POINTER(AbmForagerState), c_int32, ctypes.POINTER(AbmPatchState), c_int32,

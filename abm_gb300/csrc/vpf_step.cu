@@ -123,6 +123,43 @@ static Workspace workspace(cudaStream_t stream, int n, int words, int *status) {
     return w;
 }
 
+// Per-(device, stream) staging of abm_vpf_flock_step_host: the input state (4 n floats)
+// followed by room for the output state (used when the caller's output is not addressable).
+static float *host_staging(cudaStream_t stream, int n, int *status) {
+    static std::mutex mu;
+    static std::map<std::pair<int, void *>, std::pair<float *, long>> st;
+    static std::vector<void *> retired;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto &e = st[{dev, (void *)stream}];
+    if (e.second < n) {
+        const long cap = std::max<long>(n, 1024);
+        float *p = nullptr;
+        *status = check_cuda(cudaMalloc((void **)&p, sizeof(float) * 8 * (size_t)cap),
+                             "cudaMalloc(host staging)");
+        if (*status) return nullptr;
+        if (e.first) retired.push_back(e.first);
+        e = {p, cap};
+    }
+    *status = ABM_OK;
+    return e.first;
+}
+
+// Device-usable address of an array registered with CUDA (page-locked host memory, managed or
+// device memory), else NULL: unregistered (pageable) memory is only ever copied by the driver.
+static void *device_view(const void *host) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeManaged ||
+        at.type == cudaMemoryTypeDevice)
+        return at.devicePointer;
+    return nullptr;
+}
+
 // Per-warp work queues of the step kernel: candidate neighbours that survived the cull (their
 // positions, so the queue outlives the tile) and pairs whose FP32 decision needs the
 // double-float re-decision.
@@ -685,6 +722,17 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
     store_update(a, ku, o);
 }
 
+// Copies the four state arrays (addressable host memory) into one device staging buffer.
+__global__ void gather_state_kernel(const float *x, const float *y, const float *th,
+                                    const float *v, float *dst, int n) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        dst[k] = x[k];
+        dst[(size_t)n + k] = y[k];
+        dst[2 * (size_t)n + k] = th[k];
+        dst[3 * (size_t)n + k] = v[k];
+    }
+}
+
 // Evaluates the in-kernel double-float cos/sin (verification hook for the tests).
 __global__ void check_sincos_kernel(const float *theta, int n, double *out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1140,6 +1188,60 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     if (!ws.sums) return st;
     return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev,
                        (cudaStream_t)stream, g, sctab, ws, fn);
+}
+
+int abm_vpf_flock_step_host(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,
+                            const abm_vf_params *p, const abm_agent_overrides *ov,
+                            void *stream) {
+    const char *fn = "abm_vpf_flock_step_host";
+    int st = step_validate(in, out, n, p, fn);
+    if (st || n == 0) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const GridDev *g = grid_for(p->rv, p->fov0, p->fov1, &st);
+    if (!g) return st;
+    if ((st = ensure_sincos_table())) return st;
+    const float4 *sctab = sincos_table_dev(&st);
+    if (!sctab) return st;
+    const Workspace ws = workspace(s, n, g->words, &st);
+    if (!ws.sums) return st;
+    float *stage = host_staging(s, n, &st);
+    if (!stage) return st;
+    const float *hin[4] = {in->x, in->y, in->theta, in->v};
+    float *hout[4] = {out->x, out->y, out->theta, out->v};
+    const float *din[4];
+    float *dout[4];
+    bool zin = true, zout = true;
+    for (int k = 0; k < 4; ++k) {
+        din[k] = (const float *)device_view(hin[k]);
+        dout[k] = (float *)device_view(hout[k]);
+        zin = zin && din[k];
+        zout = zout && dout[k];
+    }
+    const size_t bytes = sizeof(float) * (size_t)n;
+    if (zin) {
+        const int blocks = std::min((n + 255) / 256, 4 * 152);
+        gather_state_kernel<<<blocks, 256, 0, s>>>(din[0], din[1], din[2], din[3], stage, n);
+        st = check_cuda(cudaGetLastError(), "gather_state_kernel launch");
+    } else {
+        for (int k = 0; k < 4 && !st; ++k)
+            st = check_cuda(cudaMemcpyAsync(stage + k * (size_t)n, hin[k], bytes,
+                                            cudaMemcpyHostToDevice, s),
+                            "cudaMemcpyAsync(state to device)");
+    }
+    if (st) return st;
+    abm_swarm_state sin{stage, stage + n, stage + 2 * (size_t)n, stage + 3 * (size_t)n};
+    float *so = stage + 4 * (size_t)n;
+    abm_swarm_state sout = zout ? abm_swarm_state{dout[0], dout[1], dout[2], dout[3]}
+                                : abm_swarm_state{so, so + n, so + 2 * (size_t)n,
+                                                  so + 3 * (size_t)n};
+    const int r = step_launch(&sin, &sout, n, p, ov, nullptr, nullptr, nullptr, s, g, sctab, ws,
+                              fn);
+    if (r < 0 || zout) return r;
+    const float *src[4] = {sout.x, sout.y, sout.theta, sout.v};
+    for (int k = 0; k < 4 && !st; ++k)
+        st = check_cuda(cudaMemcpyAsync(hout[k], src[k], bytes, cudaMemcpyDeviceToHost, s),
+                        "cudaMemcpyAsync(state to host)");
+    return st ? st : r;
 }
 
 int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32_t n_total,

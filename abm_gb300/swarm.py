@@ -138,17 +138,15 @@ class VFSwarm:
             a.velocity = float(st["v"][i])
 
 
-def step_host(lib, params_c, n, host_in, host_out, dev_in, dev_out, stream):
-    """One step on HOST pinned buffers: H2D copy, kernel, D2H copy (the drop-in call a
-    per-step host loop makes).  host_*/dev_* are dicts of float32 tensors."""
-    for k in ("x", "y", "theta", "v"):
-        dev_in[k].copy_(host_in[k], non_blocking=True)
-    st_in = VFSwarm._state_struct(dev_in)
-    st_out = VFSwarm._state_struct(dev_out)
-    status = lib.abm_vpf_flock_step(ctypes.byref(st_in), ctypes.byref(st_out), n,
-                                    ctypes.byref(params_c), None, None, None, None,
-                                    ctypes.c_void_p(stream.cuda_stream))
-    _lib.check(status, "abm_vpf_flock_step")
-    for k in ("x", "y", "theta", "v"):
-        host_out[k].copy_(dev_out[k], non_blocking=True)
+def step_host(lib, params_c, n, host_in, host_out, stream, overrides=None):
+    """One step on HOST buffers through abm_vpf_flock_step_host (the drop-in call a per-step
+    host loop makes): the library moves the state to the device and the result back, on
+    `stream`.  host_* are dicts of float32 CPU tensors (page-locked for the fast path)."""
+    st_in = VFSwarm._state_struct(host_in)
+    st_out = VFSwarm._state_struct(host_out)
+    status = lib.abm_vpf_flock_step_host(
+        ctypes.byref(st_in), ctypes.byref(st_out), n, ctypes.byref(params_c),
+        ctypes.byref(overrides) if overrides is not None else None,
+        ctypes.c_void_p(stream.cuda_stream))
+    _lib.check(status, "abm_vpf_flock_step_host")
     return status

@@ -535,21 +535,20 @@ def run_gb300(args, rank, world):
     times = np.array([a.elapsed_time(b) for a, b in ev]) * 1e-3
     kernel_s = float(times.sum())
 
-    # ---- end-to-end through the C-ABI with host buffers (H2D + step + D2H every step)
+    # ---- end-to-end through the C-ABI with host buffers (host state in, host state out
+    #      every step: abm_vpf_flock_step_host)
     host_in = {k: torch.from_numpy(state[k].copy()).pin_memory() for k in state}
     host_out = {k: torch.empty(n, dtype=torch.float32).pin_memory() for k in state}
-    dev_in = {k: torch.empty(n, dtype=torch.float32, device=dev) for k in state}
-    dev_out = {k: torch.empty(n, dtype=torch.float32, device=dev) for k in state}
     cparams = params.to_c()
     for _ in range(args.warmup):
-        step_host(lib, cparams, n, host_in, host_out, dev_in, dev_out, stream)
+        step_host(lib, cparams, n, host_in, host_out, stream)
     ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
     barrier()
     for k in range(args.steps):
         flush.fill_(float(k))
         ev2[k][0].record(stream)
-        step_host(lib, cparams, n, host_in, host_out, dev_in, dev_out, stream)
+        step_host(lib, cparams, n, host_in, host_out, stream)
         ev2[k][1].record(stream)
         host_in, host_out = host_out, host_in
     barrier()
@@ -596,8 +595,9 @@ def run_gb300(args, rank, world):
                            l2="flushed between timed steps (256 MiB write)"),
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 16 * n,
                     "d2h_bytes_per_step": 16 * n,
-                    "path": "abm_vpf_flock_step via ctypes, pinned host state, H2D + step + "
-                            "D2H each step"},
+                    "path": "abm_vpf_flock_step_host via ctypes on pinned host state: the "
+                            "input gathered from host memory by one kernel, the new state "
+                            "written to host memory by the step's last kernel, every step"},
             "gpu_launches": 2 * args.steps,   # pair kernel + update (or finish) kernel
             "roofline": roofline, "clocks": clk,
             "launch_config": dict(tuned["best"], chosen_by="abm_vpf_autotune, 5 steps per "

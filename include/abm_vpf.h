@@ -171,6 +171,20 @@ int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32
                           double *terms_dev, unsigned long long *diag_dev, void *stream);
 
 /*
+ * abm_vpf_flock_step on HOST state (no counterpart in the reference; the call a host-side
+ * loop makes once per step): in_host / out_host hold host pointers (x, y, theta, v).  For
+ * memory registered with CUDA (page-locked, e.g. cudaHostAlloc or torch pin_memory, or
+ * managed), one kernel gathers the input into a per-stream device staging buffer and the
+ * step's last kernel writes the new state straight into out_host; other (pageable) memory is
+ * copied with cudaMemcpyAsync through the same staging buffer.  Stream-ordered: the
+ * caller synchronises the stream before reading out_host.  ov (nullable) holds DEVICE arrays as
+ * for abm_vpf_flock_step.  Same status codes.
+ */
+int abm_vpf_flock_step_host(const abm_swarm_state *in_host, abm_swarm_state *out_host,
+                            int32_t n, const abm_vf_params *p, const abm_agent_overrides *ov,
+                            void *stream);
+
+/*
  * Allocation-free variant of abm_vpf_flock_step (no counterpart in the reference): the same
  * step, arguments, results and status codes, for callers that cannot call cudaMalloc, such as
  * code running inside another framework's memory pool, a host that has reserved all device

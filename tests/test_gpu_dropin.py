@@ -83,3 +83,33 @@ def test_vswrm_length_mismatch_raises_like_numpy():
     phi = np.arange(-np.pi, np.pi, 2 * np.pi / 61)      # 62 entries for Rv = 61
     with pytest.raises(ValueError):
         vf_supcalc.VSWRM_flocking_state_variables(0.0, phi, np.zeros(61), P())
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_flock_step_host_matches_device_step(pinned):
+    """abm_vpf_flock_step_host on host state (page-locked: gathered / written by the kernels;
+    pageable: copied by the driver) gives the device step's result, over several steps."""
+    import torch
+    from abm_gb300 import _lib
+    from abm_gb300.params import VFParams
+    from abm_gb300.swarm import VFSwarm, step_host
+    from _gpu_helpers import seeded_swarm
+    lib = _lib.load()
+    st = seeded_swarm(17, 900, 1500.0, 1500.0, R=5.0)
+    vp = VFParams(width=1500.0, height=1500.0, rv=1000, radius=5.0)
+    sw = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    mk = (lambda a: torch.from_numpy(f32(a)).pin_memory()) if pinned else \
+        (lambda a: torch.from_numpy(f32(a).copy()))
+    h_in = {k: mk(st[k]) for k in ("x", "y", "theta", "v")}
+    h_out = {k: mk(np.zeros_like(st[k])) for k in ("x", "y", "theta", "v")}
+    s = torch.cuda.current_stream()
+    cp = vp.to_c()
+    for _ in range(3):
+        sw.step()
+        step_host(lib, cp, len(st["x"]), h_in, h_out, s)
+        h_in, h_out = h_out, h_in
+    torch.cuda.synchronize()
+    want = sw.state_numpy()
+    for k in want:
+        assert np.array_equal(h_in[k].numpy(), want[k]), k
