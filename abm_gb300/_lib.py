@@ -96,10 +96,24 @@ FORAGER_FIELDS = (("x", c_float_p), ("y", c_float_p), ("theta", c_float_p), ("v"
                   ("collected_before", c_double_p), ("mode", c_i32_p),
                   ("override_mode", c_i32_p), ("env_status", c_i32_p),
                   ("env_status_before", c_i32_p), ("pool_success", c_i32_p),
-                  ("patch_id", c_i32_p), ("novelty", c_u32_p), ("draws", c_u64_p))
+                  ("patch_id", c_i32_p), ("novelty", c_u32_p), ("draws", c_u64_p),
+                  ("ipriv", c_double_p))
 PATCH_FIELDS = (("x", c_double_p), ("y", c_double_p), ("radius", c_double_p),
                 ("units", c_double_p), ("left", c_double_p), ("quality", c_double_p),
                 ("id", c_i32_p), ("draws", c_u64_p))
+
+
+# (field, pointer type) of abm_forage_recording after its capacity and step counter
+RECORDING_FIELDS = (("posx", c_i32_p), ("posy", c_i32_p), ("orientation", c_float_p),
+                    ("velocity", c_float_p), ("w", c_double_p), ("u", c_double_p),
+                    ("ipriv", c_double_p), ("collected", c_double_p), ("mode", c_i32_p),
+                    ("patch_id", c_i32_p), ("soc_bits", c_u32_p), ("res_posx", c_i32_p),
+                    ("res_posy", c_i32_p), ("res_left", c_double_p),
+                    ("res_quality", c_double_p), ("res_id", c_i32_p))
+
+
+class AbmForageRecording(ctypes.Structure):
+    _fields_ = [("capacity", c_int32), ("step", c_i32_p)] + list(RECORDING_FIELDS)
 
 
 class AbmForagerState(ctypes.Structure):
@@ -159,6 +173,8 @@ SIGNATURES = [
     ("abm_vpf_get_step_mode", c_int32, [c_i32_p, c_i32_p]),
     ("abm_vpf_set_step_split", c_int32, [c_int32]),
     ("abm_vpf_get_step_split", c_int32, [c_i32_p]),
+    ("abm_vpf_polarisation", c_int32,
+     [c_float_p, c_int32, c_i32_p, c_int32, c_double_p, c_int32, c_i32_p, ctypes.c_void_p]),
     ("abm_vpf_flock_step_host", c_int32,
      [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
       ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), ctypes.c_void_p]),
@@ -166,6 +182,9 @@ SIGNATURES = [
     ("abm_forage_step", c_int32,
      [ctypes.POINTER(AbmForagerState), c_int32, ctypes.POINTER(AbmPatchState), c_int32,
       ctypes.POINTER(AbmForageParams), c_u32_p, c_i32_p, c_double_p, c_u64_p, ctypes.c_void_p]),
+    ("abm_forage_record", c_int32,
+     [ctypes.POINTER(AbmForagerState), c_int32, ctypes.POINTER(AbmPatchState), c_int32, c_u32_p,
+      c_int32, ctypes.POINTER(AbmForageRecording), ctypes.c_void_p]),
     ("abm_philox4x32", None, [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                               ctypes.POINTER(ctypes.c_uint32)]),
     ("abm_vpf_autotune", c_int32,

@@ -74,6 +74,30 @@ class BatchedSweep:
         self._graph = None
         self._graph_chunk = 0
         self._stream = None
+        self._pol = None
+
+    # ------------------------------------------------------------------ ensemble statistic
+    def track_polarisation(self, capacity: int):
+        """Record each instance's polarisation (|sum (cos, sin)| / N, the reference's
+        DataLoader.calculate_polarization) after every step, on the device, for up to
+        `capacity` steps (abm_vpf_polarisation, captured with the step in graphs)."""
+        k = len(self.sizes)
+        self._pol = torch.full((k, int(capacity)), float("nan"), dtype=torch.float64,
+                               device=self.device)
+        self._pol_step = torch.zeros(k, dtype=torch.int32, device=self.device)
+        self._pol_off = torch.as_tensor(self.offsets.astype(np.int32), device=self.device)
+        self._graph = None   # re-capture with the statistic
+
+    def polarisation(self) -> np.ndarray:
+        """(n_instances, steps) polarisation series recorded so far."""
+        steps = int(self._pol_step.max().item())
+        return self._pol[:, : min(steps, self._pol.shape[1])].cpu().numpy()
+
+    def _record_polarisation(self, state, stream):
+        _lib.check(self.lib.abm_vpf_polarisation(
+            _lib.fptr(state["theta"]), self.n, _lib.i32ptr(self._pol_off), len(self.sizes),
+            _lib.dptr(self._pol), self._pol.shape[1], _lib.i32ptr(self._pol_step),
+            ctypes.c_void_p(stream.cuda_stream)), "abm_vpf_polarisation")
 
     @staticmethod
     def _state(d):
@@ -89,7 +113,10 @@ class BatchedSweep:
             ctypes.byref(self._ov), _lib.u32ptr(self.vpf_bits) if want_vpf else None,
             _lib.dptr(self.terms) if want_terms else None, _lib.u64ptr(self.diag),
             ctypes.c_void_p(stream.cuda_stream))
-        return _lib.check(status, "abm_vpf_flock_batched")
+        st = _lib.check(status, "abm_vpf_flock_batched")
+        if self._pol is not None:
+            self._record_polarisation(self._bufs[1 - src], stream)
+        return st
 
     def step(self, want_vpf=False, want_terms=False, stream=None) -> int:
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
@@ -105,12 +132,16 @@ class BatchedSweep:
         self._stream = torch.cuda.Stream(self.device)
         self._stream.wait_stream(torch.cuda.current_stream(self.device))
         saved = {k: t.clone() for k, t in self._bufs[self._cur].items()}
+        saved_pol = None if self._pol is None else (self._pol.clone(), self._pol_step.clone())
         with torch.cuda.stream(self._stream):
             for _ in range(2):     # builds tables / workspace outside the capture
                 self.step(stream=self._stream)
         self._stream.synchronize()
         for k, t in saved.items():
             self._bufs[self._cur][k].copy_(t)
+        if saved_pol is not None:   # the warm-up steps are not part of the run
+            self._pol.copy_(saved_pol[0])
+            self._pol_step.copy_(saved_pol[1])
         self._stream.wait_stream(torch.cuda.current_stream(self.device))
         g = torch.cuda.CUDAGraph()
         start = self._cur

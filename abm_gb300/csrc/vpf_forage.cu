@@ -327,6 +327,7 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
     // calc_I_priv (agent.py:180-187): novelty memory and the units collected this step
     const double I_priv = p.F_N * (a.ag.novelty[i] ? 1.0 : 0.0) +
                           p.F_R * (a.ag.collected[i] - a.ag.collected_before[i]);
+    if (a.ag.ipriv) a.ag.ipriv[i] = I_priv;
     // update_decision_processes (agent.py:194-210)
     double w = a.ag.w[i], u = a.ag.u[i];
     const double w_p = w > p.T_w ? w : 0.0;
@@ -429,6 +430,50 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
         atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
 }
 
+// ------------------------------------------------------------------------------ recording
+// One block appends column t of every series, then advances the counter.
+__global__ void __launch_bounds__(1024) forage_record_kernel(abm_forager_state ag, int n,
+                                                             abm_patch_state pt, int np,
+                                                             const uint32_t *soc, int words,
+                                                             abm_forage_recording rec) {
+    const int t = *rec.step;
+    if (t < rec.capacity) {
+        const size_t cap = (size_t)rec.capacity;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const size_t o = (size_t)i * cap + t;
+            rec.posx[o] = (int)ag.x[i];   // Python int(): truncation toward zero
+            rec.posy[o] = (int)ag.y[i];
+            rec.orientation[o] = ag.theta[i];
+            rec.velocity[o] = ag.v[i];
+            rec.w[o] = ag.w[i];
+            rec.u[o] = ag.u[i];
+            rec.ipriv[o] = ag.ipriv ? ag.ipriv[i] : 0.0;
+            rec.collected[o] = ag.collected[i];
+            const int m = ag.mode[i];   // ifdb.mode_to_int (ifdb.py:197-206)
+            rec.mode[o] = m == ABM_MODE_EXPLORE ? 0 : m == ABM_MODE_EXPLOIT ? 1
+                        : m == ABM_MODE_RELOCATE ? 2 : m == ABM_MODE_COLLIDE ? 3 : -1;
+            rec.patch_id[o] = ag.patch_id[i];
+        }
+        if (rec.soc_bits && soc) {
+            const size_t total = (size_t)n * words;
+            for (size_t q = threadIdx.x; q < total; q += blockDim.x) {
+                const size_t i = q / words, w = q % words;
+                rec.soc_bits[(i * cap + t) * words + w] = soc[q];
+            }
+        }
+        for (int k = threadIdx.x; k < np; k += blockDim.x) {
+            const size_t o = (size_t)k * cap + t;
+            rec.res_posx[o] = (int)pt.x[k];
+            rec.res_posy[o] = (int)pt.y[k];
+            rec.res_left[o] = pt.left[k];
+            rec.res_quality[o] = pt.quality[k];
+            rec.res_id[o] = pt.id[k];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *rec.step = t + 1;
+}
+
 static int forage_validate(const abm_forager_state *s, int n, const abm_patch_state *pt, int np,
                            const abm_forage_params *p, const uint32_t *soc, const int *scratch,
                            const char *fn) {
@@ -476,6 +521,27 @@ int abm_forage_params_default(abm_forage_params *p) {
     p->rv = 1200; p->fov0 = -M_PI; p->fov1 = M_PI; p->vision_range = 2000;
     p->visual_exclusion = 1; p->patchwise_exclusion = 1; p->seed = 0;
     return ABM_OK;
+}
+
+int abm_forage_record(const abm_forager_state *agents, int32_t n, const abm_patch_state *patches,
+                      int32_t n_patches, const uint32_t *soc_bits_dev, int32_t rv,
+                      abm_forage_recording *rec, void *stream) {
+    const char *fn = "abm_forage_record";
+    if (!agents || !patches || !rec || !rec->step)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: NULL argument", fn);
+    if (n < 0 || n_patches < 0 || rec->capacity < 0)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: negative size", fn);
+    if (rv < 2 || rv > ABM_MAX_RV) return set_error(ABM_ERR_RV, "%s: rv=%d", fn, rv);
+    if (n > 0 && (!rec->posx || !rec->posy || !rec->orientation || !rec->velocity || !rec->w ||
+                  !rec->u || !rec->ipriv || !rec->collected || !rec->mode || !rec->patch_id))
+        return set_error(ABM_ERR_INVALID_ARG, "%s: an agent series is NULL", fn);
+    if (n_patches > 0 && (!rec->res_posx || !rec->res_posy || !rec->res_left ||
+                          !rec->res_quality || !rec->res_id))
+        return set_error(ABM_ERR_INVALID_ARG, "%s: a patch series is NULL", fn);
+    forage_record_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(*agents, n, *patches, n_patches,
+                                                               soc_bits_dev, (rv + 31) / 32,
+                                                               *rec);
+    return check_cuda(cudaGetLastError(), "forage_record_kernel launch");
 }
 
 void abm_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {

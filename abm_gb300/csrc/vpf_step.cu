@@ -733,6 +733,42 @@ __global__ void gather_state_kernel(const float *x, const float *y, const float 
     }
 }
 
+// Polarisation of each instance (one block per instance): |sum (cos, sin)| / N.
+__global__ void __launch_bounds__(256) polarisation_kernel(const float *theta, int n_total,
+                                                           const int *offsets, double *out,
+                                                           int capacity, int *step) {
+    __shared__ double sx[8], sy[8];
+    const int k = blockIdx.x;
+    const int a0 = offsets ? offsets[k] : 0, a1 = offsets ? offsets[k + 1] : n_total;
+    double cx = 0.0, cy = 0.0;
+    for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+        float s, c;
+        sincosf(theta[i], &s, &c);
+        cx += c;
+        cy += s;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        cx += __shfl_xor_sync(ABM_FULL_MASK, cx, o);
+        cy += __shfl_xor_sync(ABM_FULL_MASK, cy, o);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sx[warp] = cx;
+        sy[warp] = cy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tx = 0.0, ty = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            tx += sx[w];
+            ty += sy[w];
+        }
+        const int t = step[k];
+        if (t < capacity && a1 > a0) out[(size_t)k * capacity + t] = sqrt(tx * tx + ty * ty) / (a1 - a0);
+        step[k] = t + 1;
+    }
+}
+
 // Evaluates the in-kernel double-float cos/sin (verification hook for the tests).
 __global__ void check_sincos_kernel(const float *theta, int n, double *out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1325,6 +1361,22 @@ int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, 
     na_ws.sums = (long long *)(d->base + kNaSums);
     return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, &d->g,
                        (const float4 *)(d->base + kNaSin), na_ws, fn);
+}
+
+int abm_vpf_polarisation(const float *theta_dev, int32_t n_total, const int32_t *offsets_dev,
+                         int32_t n_instances, double *out_dev, int32_t capacity,
+                         int32_t *step_dev, void *stream) {
+    const char *fn = "abm_vpf_polarisation";
+    if (n_total < 0 || n_instances < 0 || capacity < 0)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: negative size", fn);
+    if (!offsets_dev && n_instances != 1)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: one instance without offsets", fn);
+    if (n_instances == 0) return ABM_OK;
+    if (!theta_dev || !out_dev || !step_dev)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: NULL argument", fn);
+    polarisation_kernel<<<n_instances, 256, 0, (cudaStream_t)stream>>>(
+        theta_dev, n_total, offsets_dev, out_dev, capacity, step_dev);
+    return check_cuda(cudaGetLastError(), "polarisation_kernel launch");
 }
 
 int abm_vpf_check_sincos(const float *theta_dev, int32_t n, double *out_dev, void *stream) {

@@ -160,7 +160,8 @@ AGENT_FIELDS = (("x", np.float32), ("y", np.float32), ("theta", np.float32), ("v
                 ("collected_before", np.float64), ("mode", np.int32),
                 ("override_mode", np.int32), ("env_status", np.int32),
                 ("env_status_before", np.int32), ("pool_success", np.int32),
-                ("patch_id", np.int32), ("novelty", np.uint32), ("draws", np.uint64))
+                ("patch_id", np.int32), ("novelty", np.uint32), ("draws", np.uint64),
+                ("ipriv", np.float64))
 PATCH_FIELDS = (("x", np.float64), ("y", np.float64), ("radius", np.float64),
                 ("units", np.float64), ("left", np.float64), ("quality", np.float64),
                 ("id", np.int32), ("draws", np.uint64))
@@ -208,7 +209,8 @@ class ForagingSim:
     """One foraging arena on the GPU."""
 
     def __init__(self, params: ForageParams, n_agents: int = 100, n_patches: int = 3,
-                 init_seed: int = 0, agents=None, patches=None, device="cuda"):
+                 init_seed: int = 0, agents=None, patches=None, device="cuda",
+                 record_steps: int = 0):
         self.lib = _lib.load()
         self.params = params
         self.device = torch.device(device)
@@ -216,7 +218,9 @@ class ForagingSim:
             agents, patches = initial_state(params, n_agents, n_patches, init_seed)
         self.n = len(agents["x"])
         self.np = len(patches["x"])
-        self.ag = {k: self._dev(agents[k], dt) for k, dt in AGENT_FIELDS}
+        n0 = len(agents["x"])
+        self.ag = {k: self._dev(agents[k] if k in agents else np.zeros(n0, dt), dt)
+                   for k, dt in AGENT_FIELDS}
         self.pt = {k: self._dev(patches[k], dt) for k, dt in PATCH_FIELDS}
         self.words = int(_lib.check(self.lib.abm_vpf_words(int(params.rv)), "abm_vpf_words"))
         self.soc_bits = torch.zeros((self.n, self.words), dtype=torch.int32, device=self.device)
@@ -229,6 +233,63 @@ class ForagingSim:
             *[ctypes.cast(self.pt[k].data_ptr(), ctype) for k, ctype in _lib.PATCH_FIELDS])
         self.t = 0
         self._graph = None
+        self.rec = None
+        if record_steps > 0:
+            self._init_recording(int(record_steps))
+
+    # ------------------------------------------------------------------ recording
+    _REC_AGENT = (("posx", torch.int32), ("posy", torch.int32), ("orientation", torch.float32),
+                  ("velocity", torch.float32), ("w", torch.float64), ("u", torch.float64),
+                  ("ipriv", torch.float64), ("collected", torch.float64),
+                  ("mode", torch.int32), ("patch_id", torch.int32))
+    _REC_PATCH = (("res_posx", torch.int32), ("res_posy", torch.int32),
+                  ("res_left", torch.float64), ("res_quality", torch.float64),
+                  ("res_id", torch.int32))
+
+    def _init_recording(self, cap):
+        d = self.device
+        rec = {k: torch.zeros(self.n * cap, dtype=dt, device=d) for k, dt in self._REC_AGENT}
+        rec.update({k: torch.zeros(max(self.np, 1) * cap, dtype=dt, device=d)
+                    for k, dt in self._REC_PATCH})
+        rec["soc_bits"] = torch.zeros(self.n * cap * self.words, dtype=torch.int32, device=d)
+        rec["step"] = torch.zeros(1, dtype=torch.int32, device=d)
+        self.rec, self.rec_capacity, self.rec_t0 = rec, cap, self.t
+        self._rec_struct = _lib.AbmForageRecording(
+            cap, ctypes.cast(rec["step"].data_ptr(), _lib.c_i32_p),
+            *[ctypes.cast(rec[k].data_ptr(), c) for k, c in _lib.RECORDING_FIELDS])
+
+    def recording(self) -> dict:
+        """The recorded series on the host: agent fields (n, steps), patch fields
+        (n_patches, steps), soc_bits (n, steps, words), and the number of steps."""
+        if self.rec is None:
+            raise RuntimeError("this simulation was created without record_steps")
+        steps = min(int(self.rec["step"].item()), self.rec_capacity)
+        out = {"steps": steps, "t0": self.rec_t0}
+        for k, _ in self._REC_AGENT:
+            out[k] = self.rec[k].view(self.n, self.rec_capacity)[:, :steps].cpu().numpy()
+        for k, _ in self._REC_PATCH:
+            out[k] = self.rec[k].view(max(self.np, 1), self.rec_capacity)[:self.np, :steps] \
+                .cpu().numpy()
+        out["soc_bits"] = self.rec["soc_bits"].view(self.n, self.rec_capacity, self.words)[
+            :, :steps].cpu().numpy().view(np.uint32)
+        out["radius"] = self.pt["radius"].cpu().numpy()
+        return out
+
+    def save_reference_json(self, folder: str, env: Optional[dict] = None):
+        """Write agent_data.json, resource_data.json (and env_params.json when `env` is
+        given) in the reference's RAM-recording layout (ifdb.save_ifdb_as_csv with
+        as_zar=False, ifdb.py:412-434; env_saver.save_env_vars), readable by its DataLoader."""
+        import json
+        import os
+        os.makedirs(folder, exist_ok=True)
+        agents, resources = reference_json(self.recording(), self.params.rv)
+        with open(os.path.join(folder, "agent_data.json"), "w") as f:
+            f.write(agents)
+        with open(os.path.join(folder, "resource_data.json"), "w") as f:
+            f.write(resources)
+        if env is not None:
+            with open(os.path.join(folder, "env_params.json"), "w") as f:
+                json.dump(dict(env), f, indent=4)
 
     def _dev(self, a, dt):
         arr = np.ascontiguousarray(np.asarray(a, dt))
@@ -241,7 +302,14 @@ class ForagingSim:
             ctypes.byref(self._agent_struct), self.n, ctypes.byref(self._patch_struct), self.np,
             ctypes.byref(self._cparams), _lib.u32ptr(self.soc_bits), _lib.i32ptr(self.scratch),
             _lib.dptr(uniforms), _lib.u64ptr(self.diag), ctypes.c_void_p(stream.cuda_stream))
-        return _lib.check(status, "abm_forage_step")
+        st = _lib.check(status, "abm_forage_step")
+        if self.rec is not None:   # the reference records after the agents' update
+            _lib.check(self.lib.abm_forage_record(
+                ctypes.byref(self._agent_struct), self.n, ctypes.byref(self._patch_struct),
+                self.np, _lib.u32ptr(self.soc_bits), int(self.params.rv),
+                ctypes.byref(self._rec_struct), ctypes.c_void_p(stream.cuda_stream)),
+                "abm_forage_record")
+        return st
 
     def step(self, uniforms: Optional[torch.Tensor] = None, stream=None) -> int:
         """One step; `uniforms` (n float64 on the device) replaces the random-walk draws."""
@@ -310,6 +378,60 @@ class ForagingSim:
 
     def collected(self) -> np.ndarray:
         return self.ag["collected"].cpu().numpy()
+
+
+def _pad(number, n):
+    """ifdb.pad_to_n_digits (ifdb.py:38-52)."""
+    d = n - len(str(number))
+    return d * "0" + str(number) if d > 0 else str(number)
+
+
+def reference_json(rec: dict, rv: int):
+    """(agent_data.json, resource_data.json) text of a recording (ForagingSim.recording())
+    exactly as the reference's RAM recorder and json.dump write them (ifdb.py:55-96, :223-260,
+    :412-434): per agent its name and per-step lists, the social field stored as its rising and
+    falling edge indices in numpy's printed form; per patch id its first step, name, per-step
+    position / units left / quality and its radius."""
+    import json
+    n, steps = rec["posx"].shape
+    words = rec["soc_bits"].shape[2] if rec["soc_bits"].ndim == 3 else 0
+    agents = {}
+    for i in range(n):
+        d = {"agent_name": f"agent-{_pad(i, 2)}",
+             "posx": [int(v) for v in rec["posx"][i]], "posy": [int(v) for v in rec["posy"][i]],
+             "orientation": [float(v) for v in rec["orientation"][i]],
+             "velocity": [float(v) for v in rec["velocity"][i]],
+             "w": [float(v) for v in rec["w"][i]], "u": [float(v) for v in rec["u"][i]],
+             "Ipriv": [float(v) for v in rec["ipriv"][i]],
+             "mode": [int(v) for v in rec["mode"][i]],
+             "collectedr": [float(v) for v in rec["collected"][i]],
+             "expl_patch_id": [int(v) for v in rec["patch_id"][i]],
+             "vfield_up": [], "vfield_down": []}
+        if words:
+            by = rec["soc_bits"][i].astype("<u4").view(np.uint8).reshape(steps, -1)
+            fields = np.unpackbits(by, axis=1, bitorder="little")[:, :rv].astype(np.float64)
+            for V in fields:
+                d["vfield_up"].append(f"{np.where(np.roll(V, 1) < V)[0]}")
+                d["vfield_down"].append(f"{np.where(np.roll(V, 1) > V)[0]}")
+        agents[i] = d
+    resources = {}
+    t0 = int(rec.get("t0", 0))
+    for k in range(rec["res_id"].shape[0]):
+        for t in range(steps):
+            rid = int(rec["res_id"][k, t])
+            if rid < 0:
+                continue
+            if rid not in resources:
+                resources[rid] = {"start_time": t0 + t + 1, "end_time": None,
+                                  "res_name": f"res-{_pad(rid, 3)}", "pos_x": [], "pos_y": [],
+                                  "radius": int(rec["radius"][k]), "resc_left": [],
+                                  "quality": []}
+            r = resources[rid]
+            r["pos_x"].append(int(rec["res_posx"][k, t]))
+            r["pos_y"].append(int(rec["res_posy"][k, t]))
+            r["resc_left"].append(float(rec["res_left"][k, t]))
+            r["quality"].append(float(rec["res_quality"][k, t]))
+    return json.dumps(agents), json.dumps(resources)
 
 
 def efficiency(collected_start, collected_end, dt: float) -> np.ndarray:

@@ -75,7 +75,23 @@ class VFSwarm:
             ctypes.c_void_p(s.cuda_stream))
         self.last_status = _lib.check(status, "abm_vpf_flock_step")
         self._cur, self._nxt = self._nxt, self._cur
+        if getattr(self, "_pol", None) is not None:
+            _lib.check(self.lib.abm_vpf_polarisation(
+                _lib.fptr(self._cur["theta"]), self.n, None, 1, _lib.dptr(self._pol),
+                self._pol.shape[1], _lib.i32ptr(self._pol_step),
+                ctypes.c_void_p(s.cuda_stream)), "abm_vpf_polarisation")
         return self.last_status
+
+    def track_polarisation(self, capacity: int):
+        """Record the swarm's polarisation (|sum (cos, sin)| / N, the reference's
+        DataLoader.calculate_polarization) after every step, on the device."""
+        self._pol = torch.full((1, int(capacity)), float("nan"), dtype=torch.float64,
+                               device=self.device)
+        self._pol_step = torch.zeros(1, dtype=torch.int32, device=self.device)
+
+    def polarisation(self) -> np.ndarray:
+        steps = int(self._pol_step.item())
+        return self._pol[0, : min(steps, self._pol.shape[1])].cpu().numpy()
 
     def run(self, steps: int, stream=None) -> int:
         st = 0

@@ -73,6 +73,7 @@ typedef struct {
     int32_t *env_status, *env_status_before, *pool_success, *patch_id;
     uint32_t *novelty;                     /* bit k = novelty[k] of the reference's array */
     uint64_t *draws;                       /* random draws taken so far */
+    double *ipriv;                         /* nullable: I_priv of the last update (recording) */
 } abm_forager_state;
 
 /* Resource patches, n_patches entries per array (device). */
@@ -104,6 +105,34 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
                     int32_t n_patches, const abm_forage_params *p, uint32_t *soc_bits_dev,
                     int32_t *scratch_dev, const double *uniforms_dev,
                     unsigned long long *diag_dev, void *stream);
+
+/*
+ * Device-side recording of a run in the layout of the reference's RAM recorder
+ * (ifdb.save_agent_data_RAM / save_resource_data_RAM, abm/monitoring/ifdb.py:55-96, :223-260):
+ * agent-major series of `capacity` steps (agent i, step t at [i * capacity + t]).
+ */
+typedef struct {
+    int32_t capacity;          /* steps the series hold; later steps are not recorded */
+    int32_t *step;             /* device counter: the column of the next record */
+    int32_t *posx, *posy;      /* int(position), truncated toward zero */
+    float *orientation, *velocity;
+    double *w, *u, *ipriv, *collected;
+    int32_t *mode;             /* ifdb.mode_to_int: explore 0, exploit 1, relocate 2, collide 3 */
+    int32_t *patch_id;         /* exploited_patch_id */
+    uint32_t *soc_bits;        /* nullable: n x capacity x abm_vpf_words(rv) social fields */
+    int32_t *res_posx, *res_posy;  /* n_patches x capacity: int(position) of the slot's patch */
+    double *res_left, *res_quality;
+    int32_t *res_id;           /* n_patches x capacity: the slot's patch id (-1: no patch) */
+} abm_forage_recording;
+
+/*
+ * Append the current state of every agent and patch (and the social fields of the last step)
+ * to the recording at column *rec->step, then advance the counter (one launch; graph-safe).
+ * Call it after abm_forage_step, like the reference records after the agents' update.
+ */
+int abm_forage_record(const abm_forager_state *agents, int32_t n, const abm_patch_state *patches,
+                      int32_t n_patches, const uint32_t *soc_bits_dev, int32_t rv,
+                      abm_forage_recording *rec, void *stream);
 
 /* Philox-4x32-10 block for (counter, key): the generator of abm_forage_step, exported for
  * the tests (host function, no GPU needed). */

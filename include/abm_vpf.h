@@ -185,6 +185,19 @@ int abm_vpf_flock_step_host(const abm_swarm_state *in_host, abm_swarm_state *out
                             void *stream);
 
 /*
+ * On-device ensemble statistic (no counterpart in the reference's step; the reference computes
+ * it afterwards from recorded orientations, DataLoader.calculate_polarization,
+ * abm/loader/data_loader.py:1761-1836): the polarisation |sum_i (cos theta_i, sin theta_i)| / N
+ * of every instance of the current state, written to out_dev[k * capacity + step_dev[k]], after
+ * which step_dev[k] advances (steps beyond capacity are dropped).  offsets_dev: n_instances + 1
+ * int32 agent offsets of the instances (device; NULL: one instance of n_total agents).  One
+ * launch, graph-safe (the per-instance column counters live on the device).
+ */
+int abm_vpf_polarisation(const float *theta_dev, int32_t n_total, const int32_t *offsets_dev,
+                         int32_t n_instances, double *out_dev, int32_t capacity,
+                         int32_t *step_dev, void *stream);
+
+/*
  * Allocation-free variant of abm_vpf_flock_step (no counterpart in the reference): the same
  * step, arguments, results and status codes, for callers that cannot call cudaMalloc, such as
  * code running inside another framework's memory pool, a host that has reserved all device

@@ -121,3 +121,42 @@ def test_forage_efficiency_ensemble_matches_reference():
     se = np.sqrt(gpu.var(ddof=1) / len(gpu) + ref.var(ddof=1) / len(ref))
     assert abs(gpu.mean() - ref.mean()) <= 4 * se, (gpu.mean(), ref.mean(), se)
     assert gpu.mean() > 0.01
+
+
+def test_forage_recording_matches_states_and_graph_replay():
+    """The device recorder holds, for every step, the state after that step (modes in the
+    reference's codes, positions truncated like int()) and its social field; a graph-replayed
+    recording equals the eager one; the saved files are the reference's JSON layout."""
+    import json
+    import tempfile
+    from abm_gb300.foraging import ForageParams, ForagingSim
+    prm = ForageParams(seed=21, width=500.0, height=500.0, rv=300, min_resc_units=20,
+                       max_resc_units=60)
+    a = ForagingSim(prm, n_agents=40, n_patches=3, init_seed=4, record_steps=300)
+    b = ForagingSim(prm, n_agents=40, n_patches=3, init_seed=4, record_steps=300)
+    code = {0: 0, 2: 1, 1: 2, 4: 3}
+    states, socs = [], []
+    for _ in range(200):
+        a.step()
+        states.append(a.agents_numpy())
+        socs.append(a.soc_bits.cpu().numpy().view(np.uint32))
+    b.run(200, chunk=100)
+    ra, rb = a.recording(), b.recording()
+    assert ra["steps"] == rb["steps"] == 200
+    for k in ("posx", "posy", "orientation", "velocity", "w", "u", "ipriv", "collected",
+              "mode", "patch_id", "res_left", "res_id", "soc_bits"):
+        assert np.array_equal(ra[k], rb[k]), k
+    for t, st in enumerate(states):
+        assert np.array_equal(ra["posx"][:, t], st["x"].astype(np.int32))
+        assert np.array_equal(ra["orientation"][:, t], st["theta"])
+        assert np.array_equal(ra["collected"][:, t], st["collected"])
+        assert np.array_equal(ra["mode"][:, t], [code[int(m)] for m in st["mode"]])
+        assert np.array_equal(ra["soc_bits"][:, t], socs[t])
+    with tempfile.TemporaryDirectory() as d:
+        a.save_reference_json(d, env={"N": "40", "VISUAL_FIELD_RESOLUTION": "300"})
+        ag = json.load(open(f"{d}/agent_data.json"))
+        rs = json.load(open(f"{d}/resource_data.json"))
+        env = json.load(open(f"{d}/env_params.json"))
+    assert len(ag) == 40 and len(ag["0"]["posx"]) == 200 and ag["7"]["agent_name"] == "agent-07"
+    assert all(len(v["vfield_up"]) == len(v["vfield_down"]) == 200 for v in ag.values())
+    assert len(rs) >= 3 and env["N"] == "40"
