@@ -618,6 +618,44 @@ def run_gb300(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def profile_workload(which: str):
+    """A few eager steps of one leg's workload and nothing else: the command the ncu
+    summaries under profiles/ capture (launch lists and single-kernel captures)."""
+    import torch
+    if which == "batched":
+        from abm_gb300.batched import BatchedSweep, sweep_instances
+        from abm_gb300.params import VFParams
+        B = BATCHED
+        vp = VFParams(gam=0.1, v0=1.0, alp1=0.08, bet1=0.08, width=1000.0, height=1000.0,
+                      rv=B["rv"], radius=B["radius"])
+        b = BatchedSweep(vp, sweep_instances(n_instances=B["n_instances"], seed=B["seed"]))
+        for _ in range(8):
+            b.step()
+    elif which == "forage":
+        from abm_gb300.foraging import ForagingSim
+        sim = ForagingSim(forage_params(), n_agents=FORAGE["n_agents"],
+                          n_patches=FORAGE["n_patches"], init_seed=FORAGE["seed"])
+        for _ in range(300):
+            sim.step()
+    elif which == "edge":
+        from abm_gb300 import edge
+        from abm_gb300.params import VFParams
+        A = ADJOINT
+        rng = np.random.default_rng(A["seed"])
+        n, (W, H) = A["n_agents"], A["arena"]
+        t = lambda a: torch.tensor(a, dtype=torch.float32, device="cuda")
+        x, y = t(rng.uniform(30, 30 + W - 20, n)), t(rng.uniform(30, 30 + H - 20, n))
+        th, v = t(rng.uniform(0, 2 * np.pi, n)), t(np.zeros(n))
+        base = VFParams(width=W, height=H, radius=A["radius"], dt=A["dt"])
+        pv = torch.tensor([1.0, 0.08, 1.0, 0.08, 1.0], dtype=torch.float64, device="cuda",
+                          requires_grad=True)
+        out = edge.rollout(pv, x, y, th, v, base, 20, checkpoint=10)
+        edge.flocking_loss(out[0], out[1], out[2],
+                           torch.tensor([700.0, 700.0], device="cuda")).backward()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_workload": which, "ok": True}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -628,7 +666,12 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-forage", action="store_true")
+    ap.add_argument("--profile-workload", choices=["batched", "forage", "edge"],
+                    help="run a few eager steps of one leg's workload and exit (for ncu)")
     args = ap.parse_args()
+    if args.profile_workload:
+        profile_workload(args.profile_workload)
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
