@@ -87,7 +87,8 @@ class AbmForageParams(ctypes.Structure):
                 + [("rv", c_int32)]
                 + [(k, ctypes.c_double) for k in ("fov0", "fov1", "vision_range")]
                 + [(k, c_int32) for k in ("visual_exclusion", "patchwise_exclusion")]
-                + [("seed", ctypes.c_uint64)])
+                + [("seed", ctypes.c_uint64)]
+                + [(k, c_int32) for k in ("collide_agents", "ghost_mode")])
 
 
 # (field, pointer type) of abm_forager_state / abm_patch_state, in declaration order

@@ -2,7 +2,8 @@
 // the social visual projection field and the agent update of the reference's foraging
 // simulation, for one arena.
 //
-// Three launches per step on the caller's stream:
+// Three launches per step on the caller's stream (four with agent-agent collisions, whose
+// kernel comes first; see the collisions section):
 //  * forage_resource_kernel (one block): which patch (if any) holds each agent's centre; then
 //    one warp per patch replays the reference's per-patch loop in agent order (the loop is
 //    sequential within a patch: depletion order decides who gets the last units); then the
@@ -430,6 +431,588 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
         atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
 }
 
+// ------------------------------------------------------------------------------ collisions
+// The agent-agent block of Simulation.start (sims.py:735-784), run before the resource
+// interaction when collide_agents is set.  pygame's groupcollide lists, for every agent in
+// agent order, the agents whose rect circles overlap its own (collide_circle with the radius
+// raised by the proximity distance 2; rects hold int(position), width int(2R)).  Every listed
+// agent then makes one proximity manoeuvre (agent_agent_collision_proximity, sims.py:421-474)
+// unless ghost mode spares a pair with an exploiting member.  A manoeuvre reads only the
+// positions (unchanged in this block) and the manoeuvring agent's own heading, so an agent's
+// manoeuvres are its own sequence: as many as the lists that hold it, one after another.
+// forage_collide_kernel runs one block per agent: one pass over the other agents counts the
+// lists that hold it, decides whether it ends up among the collided agents (sims.py:756-776)
+// and collects its vicinity (the agents within 2R + 20); then the manoeuvres -- the proximity
+// field (Agent.projection_field with keep_distance_info over the full circle,
+// agent.py:457-597), the turn away from the fuller half, the stop when the 200 pixels ahead
+// are occupied -- and the collide-mode bookkeeping (sims.py:779-784).  The field's half and
+// front means are numpy means, so the sums replay numpy's pairwise summation order exactly;
+// the geometry follows the reference's FP64 operation sequence (products and sums rounded
+// separately, as numpy does them).  Only the heading changes between manoeuvres, so distance,
+// projection width and obstacle direction are computed once.
+constexpr int kCollideCap = 1024;          // agents within 2R + 20 of one agent
+
+// collide_circle on the rects: squared centre distance <= (2 (R + 2))^2, all integers (the
+// agent radius is an integer).
+__device__ inline bool rects_collide(float xa, float ya, float xb, float yb, long long half,
+                                     long long rr2) {
+    // non-finite or absurd coordinates (no rect) never collide
+    if (!(fabsf(xa) < 1e9f && fabsf(ya) < 1e9f && fabsf(xb) < 1e9f && fabsf(yb) < 1e9f))
+        return false;
+    const long long dx = ((long long)xa + half) - ((long long)xb + half);
+    const long long dy = ((long long)ya + half) - ((long long)yb + half);
+    return dx * dx + dy * dy <= rr2;
+}
+
+struct CollideEntry {
+    double d;          // centre distance (the reference's rounded FP64 value)
+    double ox, oy;     // offset from the focal centre to the obstacle centre
+    double u2x, u2y;   // its unit vector (FP64 route only)
+    unsigned long long dkey;   // bits of d: non-negative doubles order like their bits
+    float x, y;        // top-left position
+    int j;             // agent index (the reference's list order)
+    int same;          // same top-left position as the focal agent: skipped (agent.py:500)
+    int H, frac;       // proj_size / 2 = H + f: floor, and whether f > 0 (heading-independent)
+    double hp;         // proj_size / 2 in FP64 when FP32 could not decide H and f
+    int hp_exact;      // hp holds it
+    float fox, foy;    // the offset in FP32
+    int s0, e0;        // untrimmed int(t - ps/2), int(t + ps/2) under the current heading
+    int fov;           // bearing inside (-pi, pi)
+    int redo;          // FP32 bearing too close to a decision boundary: FP64 route
+    int r0l, r0h, r1l, r1h, r2l, r2h;   // fill ranges: wrap below 0 (1), wrap above Rv (1),
+                                         // main run (w), numpy slice bounds
+};
+
+// int(t - ps/2), int(t + ps/2) for an integer pixel t (truncation toward zero,
+// agent.py:545-548): from ps/2 = H + f with f far from 0 and 1, or from the FP64 value.
+__device__ __forceinline__ void proj_interval(int t, const CollideEntry &E, int &s0, int &e0) {
+    if (E.hp_exact) {
+        s0 = (int)__dsub_rn((double)t, E.hp);
+        e0 = (int)__dadd_rn((double)t, E.hp);
+    } else {
+        s0 = (E.frac && t - E.H >= 1) ? t - E.H - 1 : t - E.H;
+        e0 = t + E.H;
+    }
+}
+
+struct CollideSmem {
+    size_t ent, rank, code, val, nodes, total;
+};
+
+static __host__ __device__ __forceinline__ size_t collide_align16(size_t b) {
+    return (b + 15) & ~size_t(15);
+}
+
+constexpr int kCollideMaxLeaves = 3 * 160;   // pairwise leaves of three slices of <= 8192
+constexpr int kCollideMaxNodes = 2 * kCollideMaxLeaves;
+
+// Dynamic shared memory of forage_collide_kernel: entries, fill order, pixel codes, the
+// pairwise trees' node values, and the node table (leaf start / length, children, level).
+static __host__ __device__ __forceinline__ CollideSmem collide_smem(int rv, int cap) {
+    CollideSmem l;
+    l.ent = 0;
+    l.rank = collide_align16((size_t)cap * sizeof(CollideEntry));
+    l.code = collide_align16(l.rank + (size_t)cap * sizeof(int));
+    l.val = collide_align16(l.code + (size_t)rv);
+    // node values, then the per-pixel writer array of the fills
+    l.nodes = collide_align16(l.val + (size_t)kCollideMaxNodes * sizeof(double) +
+                              (size_t)rv * sizeof(int));
+    l.total = collide_align16(l.nodes + (size_t)kCollideMaxNodes * 4 * sizeof(int));
+    return l;
+}
+
+// numpy slice bounds a[lo:hi] on n elements (negative indices count from the end, clamped).
+__device__ __forceinline__ void np_slice_bounds(long long lo, long long hi, int n, int &l, int &h) {
+    if (lo < 0) { lo += n; if (lo < 0) lo = 0; }
+    if (hi < 0) { hi += n; if (hi < 0) hi = 0; }
+    if (lo > n) lo = n;
+    if (hi > n) hi = n;
+    l = (int)lo;
+    h = (int)hi;
+}
+
+// supcalc.unit_vector (supcalc.py:14-16): v / np.linalg.norm(v), products and sums rounded
+// separately.
+__device__ __forceinline__ void unit_vector_f64(double vx, double vy, double &ux, double &uy) {
+    const double nrm = __dsqrt_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)));
+    ux = __ddiv_rn(vx, nrm);
+    uy = __ddiv_rn(vy, nrm);
+}
+
+// supcalc.angle_between on unit vectors + the strict closed-angle rule of
+// Agent.projection_field (supcalc.py:19-34, agent.py:515-523).  The angle lies in [-pi, pi],
+// so numpy's remainder by 2 pi is the angle itself, plus 2 pi when negative.
+__device__ __forceinline__ double closed_angle_unit_f64(double u1x, double u1y, double u2x,
+                                                        double u2y) {
+    double dot = __dadd_rn(__dmul_rn(u1x, u2x), __dmul_rn(u1y, u2y));
+    if (dot < -1.0) dot = -1.0;
+    if (dot > 1.0) dot = 1.0;
+    double ang = acos(dot);
+    if (__dsub_rn(__dmul_rn(u1x, u2y), __dmul_rn(u1y, u2x)) < 0) ang = -ang;
+    const double tp = 2 * kPi;
+    const double c = ang < 0 ? __dadd_rn(ang, tp) : (ang == 0 ? 0.0 : ang);
+    return (0 < c && c < kPi) ? -c : __dsub_rn(tp, c);
+}
+
+// numpy's pairwise summation tree over [lo, lo + n) (split at half the length rounded down to
+// a multiple of 8, leaves of at most 128 elements): leaves get node ids in left-to-right order
+// from 0 (n0 = start, n1 = length), internal nodes (n0, n1 = left and right child) ids from
+// kCollideMaxLeaves, each after its children; n2 = level (0 for a leaf).  Returns the root id.
+__device__ int pw_tree(int lo, int n, int4 *node, int *nleaf, int *nnode) {
+    int so[32], sl[32], st[32], sleft[32], sp = 0, ret = -1;
+    so[sp] = lo; sl[sp] = n; st[sp++] = 0;
+    while (sp) {
+        const int t = sp - 1;
+        if (sl[t] <= 128) {
+            ret = (*nleaf)++;
+            node[ret] = make_int4(so[t], sl[t], 0, 0);
+            --sp;
+            continue;
+        }
+        int n2 = sl[t] / 2;
+        n2 -= n2 % 8;
+        if (st[t] == 0) {
+            st[t] = 1;
+            so[sp] = so[t]; sl[sp] = n2; st[sp++] = 0;
+        } else if (st[t] == 1) {
+            sleft[t] = ret;
+            st[t] = 2;
+            so[sp] = so[t] + n2; sl[sp] = sl[t] - n2; st[sp++] = 0;
+        } else {
+            const int id = (*nnode)++;
+            node[id] = make_int4(sleft[t], ret, max(node[sleft[t]].z, node[ret].z) + 1, 0);
+            ret = id;
+            --sp;
+        }
+    }
+    return ret;
+}
+
+constexpr int kCollideBlock = 256;
+
+__global__ void __launch_bounds__(kCollideBlock) forage_collide_kernel(ForageArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_m, s_over, s_cnt, s_any, s_both, s_nleaf, s_nnode, s_maxlv, s_root[3];
+    __shared__ int s_redo, s_slow, s_occ, s_cnt6[6];
+    __shared__ float s_thf;
+    __shared__ double s_w, s_th, s_D, s_u1[2], s_sum[3], s_mean[2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nthr = blockDim.x;
+    const int i = blockIdx.x;
+    const int rv = a.p.rv;
+    const double R = a.p.agent_radius;
+    const bool ghost = a.p.ghost_mode != 0;
+    const bool ei = a.ag.override_mode[i] == ABM_MODE_EXPLOIT;
+    const int cap = min(a.n, kCollideCap);
+    const CollideSmem L = collide_smem(rv, cap);
+    CollideEntry *ent = reinterpret_cast<CollideEntry *>(smem + L.ent);
+    int *rank = reinterpret_cast<int *>(smem + L.rank);
+    unsigned char *code = smem + L.code;
+    double *val = reinterpret_cast<double *>(smem + L.val);
+    int4 *node = reinterpret_cast<int4 *>(smem + L.nodes);
+    if (tid == 0) {
+        s_m = 0;
+        s_over = 0;
+        s_cnt = 0;
+        s_any = 0;
+        s_both = 0;
+        s_redo = 0;
+        s_slow = 0;
+        s_occ = 0;
+        s_D = -1.0;
+        for (int q = 0; q < 6; ++q) s_cnt6[q] = 0;
+        s_th = (double)a.ag.theta[i];
+        s_thf = a.ag.theta[i];
+    }
+    __syncthreads();
+    // ---- one pass over the other agents: the collision lists that hold i (pygame's
+    //      groupcollide: rect circles, radius + 2), and the vicinity of the proximity field
+    //      (supcalc.distance(agent, agent2) < 2 R + 20, sims.py:446) with what does not depend
+    //      on the heading: distance, projection half size, direction
+    const long long halfw = (long long)(2 * R) / 2;
+    const long long rr2 = (long long)(2 * R + 4) * (long long)(2 * R + 4);
+    const float fx = a.ag.x[i], fy = a.ag.y[i];
+    const double xi = fx, yi = fy;
+    const double c1x = __dadd_rn(xi, R), c1y = __dadd_rn(yi, R);
+    const double tp = 2 * kPi;
+    {
+        int cnt = 0, any = 0, both = 0;
+        for (int j = tid; j < a.n; j += nthr) {
+            if (j == i) continue;
+            const float xj = a.ag.x[j], yj = a.ag.y[j];
+            if (rects_collide(fx, fy, xj, yj, halfw, rr2)) {
+                const bool ej = a.ag.override_mode[j] == ABM_MODE_EXPLOIT;
+                if (!(ghost && (ei || ej))) ++cnt;
+                any = 1;
+                if (!ei && !ej) both = 1;
+            }
+            // FP32 screen (the offsets' squares are far from the threshold, or FP64 decides)
+            const float fdx = xj - fx, fdy = yj - fy, lim = (float)(2 * R + 20) + 1.f;
+            if (fdx * fdx + fdy * fdy > lim * lim) continue;
+            const double ddx = __dsub_rn(__dadd_rn((double)xj, R), c1x);
+            const double ddy = __dsub_rn(__dadd_rn((double)yj, R), c1y);
+            const double d = __dsqrt_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)));
+            if (!(d < 2 * R + 20)) continue;
+            const int pos = atomicAdd(&s_m, 1);
+            if (pos >= cap) {
+                s_over = 1;
+                continue;
+            }
+            CollideEntry e;
+            e.d = d;
+            e.x = xj;
+            e.y = yj;
+            e.j = j;
+            e.same = xj == fx && yj == fy;
+            e.ox = ddx;
+            e.oy = ddy;
+            e.dkey = (unsigned long long)__double_as_longlong(d);
+            e.fov = 0;
+            ent[pos] = e;
+        }
+        cnt = __reduce_add_sync(ABM_FULL_MASK, cnt);
+        any = __reduce_or_sync(ABM_FULL_MASK, any);
+        both = __reduce_or_sync(ABM_FULL_MASK, both);
+        if (lane == 0) {
+            if (cnt) atomicAdd(&s_cnt, cnt);
+            if (any) atomicOr(&s_any, 1);
+            if (both) atomicOr(&s_both, 1);
+        }
+    }
+    __syncthreads();
+    const int cnt = s_cnt;
+    // collided_agents (sims.py:756-776): teleport_exploit keeps the non-exploiting members of
+    // every colliding pair; otherwise both members, in ghost mode only pairs without exploiter
+    const bool coll = a.p.teleport_exploit ? (!ei && s_any) : (!ghost ? s_any != 0 : s_both != 0);
+    float v_new = a.ag.v[i];
+    if (cnt > 0) {   // block-uniform
+        const int h = rv / 2;
+        int flo, fhi;
+        np_slice_bounds((long long)h - 100, (long long)h + 100, rv, flo, fhi);
+        const int m = min(s_m, cap);
+        if (tid == 0) {
+            s_nleaf = -1;   // the pairwise trees are built on first use
+            // `distance` after the obstacle loop: the last non-coincident obstacle in list order
+            int jl = -1;
+            double dl = 0.0;
+            for (int e = 0; e < m; ++e) {
+                if (!ent[e].same && ent[e].j > jl) {
+                    jl = ent[e].j;
+                    dl = ent[e].d;
+                }
+            }
+            s_w = __dsub_rn(1.0, __ddiv_rn(dl, a.p.vision_range));
+            if (s_over && a.diag) atomicAdd(&a.diag[ABM_DIAG_CAPACITY], 1ull);
+        }
+        // fill order = the reference's stable sorts (distance ascending, then visual angle
+        // descending): ascending (distance, list index); and what does not depend on the
+        // heading: ps/2 = (2 atan(R / d) / (2 pi)) * Rv / 2 (agent.py:529-566) matters only
+        // through its floor H and whether it has a fraction -- FP32 decides them outside a
+        // relative guard of 4e-6 (its error is below 1e-6), the reference's FP64 sequence
+        // inside it
+        const float hp_scale = (float)((double)rv / tp);
+        for (int e = tid; e < m; e += nthr) {
+            CollideEntry &E = ent[e];
+            if (!E.same) {
+                const float hpf = atanf((float)R / (float)E.d) * hp_scale;
+                const float fl = floorf(hpf), fr = hpf - fl, g = 4e-6f * hpf + 1e-6f;
+                E.H = (int)fl;
+                E.frac = 1;
+                E.hp_exact = !(fr > g && fr < 1.f - g);
+                if (E.hp_exact) {
+                    const double va = __dmul_rn(2.0, atan(__ddiv_rn(R, E.d)));
+                    E.hp = __ddiv_rn(__dmul_rn(__ddiv_rn(va, tp), (double)rv), 2.0);
+                }
+                E.fox = (float)E.ox;
+                E.foy = (float)E.oy;
+            }
+            const unsigned long long de = E.dkey;
+            const int je = E.j;
+            int r = 0;
+            for (int q = 0; q < m; ++q)
+                r += (ent[q].dkey < de) || (ent[q].dkey == de && ent[q].j < je);
+            rank[r] = e;
+        }
+        __syncthreads();
+        const double step = __ddiv_rn(__dsub_rn(kPi, -kPi), (double)(rv - 1));
+        const float inv_stepf = (float)(1.0 / step), stepf = (float)step;
+        int *writer = reinterpret_cast<int *>(val + kCollideMaxNodes);   // after the node values
+        // FP32 bearing guard: the FP32 angle is within 1.5e-6 rad of the exact one (heading
+        // rounded to float, sincosf, products, atan2f); decisions closer than this to a pixel
+        // boundary or to the field's limits are taken again on the FP64 route
+        constexpr float kGuard = 4e-6f;
+        for (int it = 0; it < cnt; ++it) {
+            // ---- bearing, nearest pixel and untrimmed interval per entry: FP32 first
+            {
+                float sf, cf;
+                sincosf(s_thf, &sf, &cf);
+                for (int e = tid; e < m; e += nthr) {
+                    CollideEntry &E = ent[e];
+                    E.fov = 0;
+                    E.redo = 0;
+                    if (E.same) continue;
+                    const float dx = E.fox, dy = E.foy;
+                    // angle_between(v1, v2) with v1 ~ (cos th, -sin th): atan2(cross, dot)
+                    const float dot = cf * dx - sf * dy, cross = cf * dy + sf * dx;
+                    const float ang = atan2f(cross, dot);
+                    const float aa = fabsf(ang);
+                    const float u = (-ang + kPiF) * inv_stepf;   // closed angle = -angle
+                    const float fr = u - floorf(u);
+                    if (aa < kGuard || aa > kPiF - kGuard ||
+                        fabsf(fr - 0.5f) * stepf < kGuard) {
+                        E.redo = 1;
+                        s_redo = 1;
+                        if (a.diag) atomicAdd(&a.diag[ABM_DIAG_COLLIDE_FP64], 1ull);
+                        continue;
+                    }
+                    const int t = min(max((int)floorf(u + 0.5f), 0), rv - 1);
+                    proj_interval(t, E, E.s0, E.e0);
+                    E.fov = 1;
+                }
+                for (int p = tid; p < rv; p += nthr) writer[p] = -1;
+            }
+            __syncthreads();
+            if (s_redo) {   // block-uniform: the FP64 route of the reference (agent.py:486-571)
+                if (tid == 0) {
+                    double sn, cs;
+                    sincos(s_th, &sn, &cs);
+                    const double v1x =
+                        __dsub_rn(__dadd_rn(xi, __dmul_rn(__dadd_rn(1.0, cs), R)), c1x);
+                    const double v1y =
+                        __dsub_rn(__dadd_rn(yi, __dmul_rn(__dsub_rn(1.0, sn), R)), c1y);
+                    unit_vector_f64(v1x, v1y, s_u1[0], s_u1[1]);
+                }
+                __syncthreads();
+                const double u1x = s_u1[0], u1y = s_u1[1];
+                for (int e = tid; e < m; e += nthr) {
+                    CollideEntry &E = ent[e];
+                    if (!E.redo) continue;
+                    unit_vector_f64(E.ox, E.oy, E.u2x, E.u2y);
+                    const double ca = closed_angle_unit_f64(u1x, u1y, E.u2x, E.u2y);
+                    if (!(-kPi < ca && ca < kPi)) continue;   // outside the full-circle FOV
+                    // supcalc.find_nearest on np.linspace(-pi, pi, rv): argmin, first on ties
+                    const double kf = floor((ca + kPi) * (1.0 / step) + 0.5);
+                    const int k0 = (int)fmin(fmax(kf, 0.0), (double)(rv - 1));
+                    double best = INFINITY;
+                    int t = 0;
+                    for (int k = max(k0 - 2, 0); k <= min(k0 + 2, rv - 1); ++k) {
+                        const double ph =
+                            k == rv - 1 ? kPi : __dadd_rn(__dmul_rn((double)k, step), -kPi);
+                        const double dd = fabs(__dsub_rn(ph, ca));
+                        if (dd < best) {
+                            best = dd;
+                            t = k;
+                        }
+                    }
+                    proj_interval(t, E, E.s0, E.e0);
+                    E.fov = 1;
+                }
+                __syncthreads();
+                if (tid == 0) s_redo = 0;
+            }
+            // ---- exclusion trimming against the strictly closer entries (agent.py:421-445),
+            //      then the entry's fill ranges (agent.py:576-588)
+            for (int r = tid; r < m; r += nthr) {
+                CollideEntry &F = ent[rank[r]];
+                if (!F.fov) continue;
+                int sx = F.s0, ex = F.e0;
+                if (a.p.visual_exclusion) {
+                    for (int q = 0; q < r; ++q) {
+                        const CollideEntry &I = ent[rank[q]];
+                        if (!I.fov || !(I.dkey < F.dkey)) continue;
+                        if (sx <= I.s0 && I.s0 <= ex) ex = I.s0;
+                        if (sx <= I.e0 && I.e0 <= ex) sx = I.e0;
+                        if (I.s0 <= sx && I.e0 >= ex) {
+                            sx = 0;
+                            ex = 0;
+                        }
+                    }
+                }
+                F.r0l = F.r0h = F.r1l = F.r1h = 0;
+                if (sx < 0) {
+                    np_slice_bounds((long long)rv + sx, rv, rv, F.r0l, F.r0h);
+                    sx = 0;
+                }
+                if (ex >= rv) {
+                    np_slice_bounds(0, (long long)ex - rv, rv, F.r1l, F.r1h);
+                    ex = rv - 1;
+                }
+                np_slice_bounds(sx, ex, rv, F.r2l, F.r2h);
+            }
+            __syncthreads();
+            // ---- the fills in rank order, last write wins: each pixel keeps the largest
+            //      (rank, part) that writes it; parts in write order: wrap below 0, wrap above
+            //      Rv (both 1), main run (w)
+            for (int r = 0; r < m; ++r) {
+                const CollideEntry &E = ent[rank[r]];
+                if (!E.fov) continue;
+                for (int p = E.r0l + tid; p < E.r0h; p += nthr) atomicMax(&writer[p], 4 * r);
+                for (int p = E.r1l + tid; p < E.r1h; p += nthr) atomicMax(&writer[p], 4 * r + 1);
+                for (int p = E.r2l + tid; p < E.r2h; p += nthr) atomicMax(&writer[p], 4 * r + 2);
+            }
+            __syncthreads();
+            // ---- pixel codes (0 empty, 1 one, 2 w) and their counts in the two halves and the
+            //      200 pixels ahead; element k of the stored field is raw pixel rv - 1 - k
+            {
+                int l1 = 0, l2 = 0, r1 = 0, r2 = 0, f1 = 0, f2 = 0;   // ones / w's per slice
+                for (int p = tid; p < rv; p += nthr) {
+                    const int wr = writer[p];
+                    const unsigned char cd = wr < 0 ? 0 : ((wr & 3) == 2 ? 2 : 1);
+                    code[p] = cd;
+                    if (cd) {
+                        const int k = rv - 1 - p;
+                        const int one = cd == 1, ww = cd == 2;
+                        if (k < h) { l1 += one; l2 += ww; } else { r1 += one; r2 += ww; }
+                        if (flo <= k && k < fhi) { f1 += one; f2 += ww; }
+                    }
+                }
+                const int cs[6] = {l1, l2, r1, r2, f1, f2};
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    const int v = __reduce_add_sync(ABM_FULL_MASK, cs[q]);
+                    if (lane == 0 && v) atomicAdd(&s_cnt6[q], v);
+                }
+            }
+            __syncthreads();
+            // ---- the manoeuvre.  D = np.sign(mean(left) - mean(right)) (0 -> -1) and the
+            //      front test mean(ahead) > 0 follow from the exact sums (counts x {1, w}) when
+            //      they are farther apart than numpy's rounding can move them (pairwise sums
+            //      of <= 8192 terms: < 40 eps relative); otherwise numpy's sums are replayed
+            if (tid == 0) {
+                const double w = s_w, aw = fabs(w);
+                const double cl1 = s_cnt6[0], cl2 = s_cnt6[1], cr1 = s_cnt6[2], cr2 = s_cnt6[3];
+                const double cf1 = s_cnt6[4], cf2 = s_cnt6[5];
+                int slow = 0;
+                double D = -1.0;
+                if (cl1 + cl2 + cr1 + cr2 > 0) {
+                    const double A = (cl1 + cl2 * w) * (double)(rv - h);
+                    const double B = (cr1 + cr2 * w) * (double)h;
+                    const double mag = (cl1 + cl2 * aw) * (double)(rv - h) + (cr1 + cr2 * aw) * h;
+                    if (fabs(A - B) > 1e-12 * mag) D = A > B ? 1.0 : -1.0;
+                    else slow |= 1;
+                }
+                bool occupied = false;
+                if (fhi > flo && cf1 + cf2 > 0) {
+                    if (w >= 0 || cf2 == 0) {
+                        occupied = cf1 > 0 || w > 0;
+                    } else {
+                        const double S = cf1 + cf2 * w;
+                        if (fabs(S) > 1e-12 * (cf1 + cf2 * aw)) occupied = S > 0;
+                        else slow |= 2;
+                    }
+                }
+                s_slow = slow;
+                if (slow && a.diag) atomicAdd(&a.diag[ABM_DIAG_COLLIDE_REPLAYS], 1ull);
+                s_D = D;
+                s_occ = occupied;
+                for (int q = 0; q < 6; ++q) s_cnt6[q] = 0;
+            }
+            __syncthreads();
+            if (s_slow) {   // block-uniform: numpy's pairwise sums, replayed exactly
+                const bool build = s_nleaf < 0;   // the three slices' pairwise trees, once
+                __syncthreads();                  // (every thread has read the flag)
+                if (build) {
+                    if (tid == 0) {
+                        int nl = 0, nn = kCollideMaxLeaves;
+                        s_root[0] = pw_tree(0, h, node, &nl, &nn);
+                        s_root[1] = pw_tree(h, rv - h, node, &nl, &nn);
+                        s_root[2] = fhi > flo ? pw_tree(flo, fhi - flo, node, &nl, &nn) : -1;
+                        int mx = 0;
+                        for (int q = kCollideMaxLeaves; q < nn; ++q) mx = max(mx, node[q].z);
+                        s_nnode = nn;
+                        s_maxlv = mx;
+                        s_nleaf = nl;
+                    }
+                    __syncthreads();
+                }
+                const int nleaf = s_nleaf, nnode = s_nnode, maxlv = s_maxlv;
+                // eight lanes per leaf run its eight accumulators (adding 0.0 is skipped: exact)
+                const double w = s_w;
+                const int g = lane >> 3, jj = lane & 7;
+                for (int base = warp * 4; base < nleaf; base += (nthr >> 5) * 4) {
+                    const int q = base + g;
+                    const bool act = q < nleaf;
+                    const int lo = act ? node[q].x : 0, n = act ? node[q].y : 0;
+                    double r = 0.0;
+                    if (act && n >= 8) {
+                        const unsigned char c0 = code[rv - 1 - (lo + jj)];
+                        r = c0 == 0 ? 0.0 : (c0 == 1 ? 1.0 : w);
+                        for (int k = 8; k < n - (n % 8); k += 8) {
+                            const unsigned char c = code[rv - 1 - (lo + k + jj)];
+                            if (c) r = __dadd_rn(r, c == 1 ? 1.0 : w);
+                        }
+                    }
+                    // ((r0 + r1) + (r2 + r3)) + ((r4 + r5) + (r6 + r7)): IEEE addition commutes
+                    r = __dadd_rn(r, __shfl_xor_sync(ABM_FULL_MASK, r, 1));
+                    r = __dadd_rn(r, __shfl_xor_sync(ABM_FULL_MASK, r, 2));
+                    r = __dadd_rn(r, __shfl_xor_sync(ABM_FULL_MASK, r, 4));
+                    if (act && jj == 0) {
+                        int k = n >= 8 ? n - (n % 8) : 0;
+                        double res = n >= 8 ? r : 0.0;
+                        for (; k < n; ++k) {
+                            const unsigned char c = code[rv - 1 - (lo + k)];
+                            if (c) res = __dadd_rn(res, c == 1 ? 1.0 : w);
+                        }
+                        val[q] = res;
+                    }
+                }
+                __syncthreads();
+                // the trees' internal nodes level by level (left + right), then the means
+                if (warp == 0) {
+                    for (int lv = 1; lv <= maxlv; ++lv) {
+                        for (int q = kCollideMaxLeaves + lane; q < nnode; q += 32) {
+                            const int4 nd = node[q];
+                            if (nd.z == lv) val[q] = __dadd_rn(val[nd.x], val[nd.y]);
+                        }
+                        __syncwarp();
+                    }
+                    if (lane < 3) {
+                        const int root = s_root[lane];
+                        // np.mean: (0 + pairwise sum) / n
+                        s_sum[lane] = root >= 0 ? __dadd_rn(0.0, val[root]) : 0.0;
+                        if (lane < 2)
+                            s_mean[lane] = __ddiv_rn(s_sum[lane], (double)(lane == 0 ? h : rv - h));
+                    }
+                    __syncwarp();
+                    if (lane == 0) {
+                        if (s_slow & 1) s_D = s_mean[0] > s_mean[1] ? 1.0 : -1.0;
+                        if (s_slow & 2) s_occ = fhi > flo && s_sum[2] > 0;
+                        s_slow = 0;
+                    }
+                }
+                __syncthreads();
+            }
+            if (tid == 0) {
+                if (!ei) s_th = __dsub_rn(s_th, s_D * 0.2);
+                s_thf = (float)s_th;
+                if (s_occ) v_new = 0.0f;
+                else if (!ei) v_new = (float)a.p.exp_vel_max;
+            }
+            __syncthreads();
+        }
+    }
+    if (tid != 0) return;
+    if (cnt > 0) {
+        if (!ei) {
+            a.ag.override_mode[i] = ABM_MODE_COLLIDE;
+            a.ag.mode[i] = ABM_MODE_COLLIDE;
+        }
+        a.ag.theta[i] = (float)s_th;
+        a.ag.v[i] = v_new;
+    }
+    // sims.py:779-784: collide mode ends when the agent is not among the collided ones; a
+    // collided agent still in collide mode is notified with -1
+    const bool in_collide = a.ag.override_mode[i] == ABM_MODE_COLLIDE;
+    if (!coll && in_collide) {
+        a.ag.override_mode[i] = ABM_MODE_NONE;
+        a.ag.mode[i] = ABM_MODE_EXPLORE;
+    }
+    if (coll && in_collide) notify(a, i, -1, -1);
+}
+
+static size_t collide_smem_bytes(int rv, int n) {
+    return collide_smem(rv, std::min(n, kCollideCap)).total;
+}
+
 // ------------------------------------------------------------------------------ recording
 // One block appends column t of every series, then advances the counter.
 __global__ void __launch_bounds__(1024) forage_record_kernel(abm_forager_state ag, int n,
@@ -486,6 +1069,9 @@ static int forage_validate(const abm_forager_state *s, int n, const abm_patch_st
     if (p->rv < 2 || p->rv > ABM_MAX_RV) return set_error(ABM_ERR_RV, "%s: rv=%d", fn, p->rv);
     if (!(p->agent_radius > 0) || !(p->width > 0) || !(p->height > 0))
         return set_error(ABM_ERR_INVALID_ARG, "%s: radius / arena not positive", fn);
+    if (p->collide_agents && (p->agent_radius != floor(p->agent_radius) || p->agent_radius > 1e6))
+        return set_error(ABM_ERR_INVALID_ARG,
+                         "%s: agent collisions need an integer agent_radius (pygame rects)", fn);
     if (n == 0) return ABM_OK;
     const void *need[] = {s->x, s->y, s->theta, s->v, s->w, s->u, s->collected,
                           s->collected_before, s->mode, s->override_mode, s->env_status,
@@ -520,6 +1106,7 @@ int abm_forage_params_default(abm_forage_params *p) {
     p->min_resc_quality = 1; p->max_resc_quality = 1; p->patch_radius = 30;
     p->rv = 1200; p->fov0 = -M_PI; p->fov1 = M_PI; p->vision_range = 2000;
     p->visual_exclusion = 1; p->patchwise_exclusion = 1; p->seed = 0;
+    p->collide_agents = 0; p->ghost_mode = 1;
     return ABM_OK;
 }
 
@@ -569,6 +1156,16 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
     a.exploit = scratch_dev + n;
     a.uniforms = uniforms_dev;
     a.diag = diag_dev;
+    if (p->collide_agents) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(forage_collide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024);
+            attr = true;
+        }
+        forage_collide_kernel<<<n, kCollideBlock, collide_smem_bytes(p->rv, n), s>>>(a);
+        if ((st = check_cuda(cudaGetLastError(), "forage_collide_kernel launch"))) return st;
+    }
     forage_resource_kernel<<<1, kResourceThreads, 0, s>>>(a);
     if ((st = check_cuda(cudaGetLastError(), "forage_resource_kernel launch"))) return st;
     st = abm_vpf_social_fields(agents->x, agents->y, agents->theta, nullptr, p->agent_radius,

@@ -74,6 +74,9 @@ class ForageParams:
     visual_exclusion: bool = True
     patchwise_exclusion: bool = True
     seed: int = 0
+    # agent-agent collisions (AGENT_AGENT_COLLISION, GHOST_WHILE_EXPLOIT of the root .env)
+    collide_agents: bool = False
+    ghost_mode: bool = True
 
     _FP = ("T_w", "Eps_w", "g_w", "B_w", "w_max", "T_u", "Eps_u", "g_u", "B_u", "u_max", "S_wu",
            "S_uw", "F_N", "F_R", "exp_vel_max", "exp_theta_min", "exp_theta_max",
@@ -81,7 +84,7 @@ class ForageParams:
            "consumption", "min_resc_quality", "max_resc_quality", "patch_radius")
     _IP = ("Tau", "pooling_time", "teleport_exploit", "regenerate_patches",
            "allow_border_patch_overlap", "min_resc_units", "max_resc_units", "rv",
-           "visual_exclusion", "patchwise_exclusion")
+           "visual_exclusion", "patchwise_exclusion", "collide_agents", "ghost_mode")
 
     def to_c(self) -> "_lib.AbmForageParams":
         c = _lib.AbmForageParams()
@@ -95,7 +98,7 @@ class ForageParams:
         return c
 
     def oracle_arrays(self):
-        """(FP[30], IP[10], seed) in the layout of the oracle's orc_forage_step."""
+        """(FP[30], IP[12], seed) in the layout of the oracle's orc_forage_step."""
         fp = [float(getattr(self, k)) for k in self._FP]
         fp += [-self.fov * math.pi, self.fov * math.pi, float(self.vision_range)]
         ip = [int(getattr(self, k)) for k in self._IP]
@@ -103,11 +106,14 @@ class ForageParams:
 
     @classmethod
     def from_arrays(cls, fp, ip, seed: int = 0) -> "ForageParams":
-        """Inverse of oracle_arrays()."""
+        """Inverse of oracle_arrays() (arrays without the two collision switches leave
+        collisions off)."""
         kw = {k: float(fp[j]) for j, k in enumerate(cls._FP)}
-        kw.update({k: int(ip[j]) for j, k in enumerate(cls._IP)})
+        kw.update({k: int(ip[j]) for j, k in enumerate(cls._IP) if j < len(ip)})
         for k in ("teleport_exploit", "regenerate_patches", "allow_border_patch_overlap",
-                  "visual_exclusion", "patchwise_exclusion"):
+                  "visual_exclusion", "patchwise_exclusion", "collide_agents", "ghost_mode"):
+            if k not in kw:
+                continue
             kw[k] = bool(kw[k])
         fov0, fov1, vr = (float(v) for v in fp[len(cls._FP):len(cls._FP) + 3])
         return cls(**kw, fov=fov1 / math.pi, vision_range=vr, seed=int(seed))
@@ -146,7 +152,9 @@ class ForageParams:
                 vision_range=i("VISION_RANGE", d.vision_range),
                 visual_exclusion=bool(i("VISUAL_EXCLUSION", d.visual_exclusion)),
                 patchwise_exclusion=bool(i("PATCHWISE_SOCIAL_EXCLUSION",
-                                           d.patchwise_exclusion)))
+                                           d.patchwise_exclusion)),
+                collide_agents=bool(i("AGENT_AGENT_COLLISION", d.collide_agents)),
+                ghost_mode=bool(i("GHOST_WHILE_EXPLOIT", d.ghost_mode)))
         # sims.py:176-179: a negative maximum means a constant (units: randint(min, min + 1))
         if p.max_resc_quality < 0:
             p.max_resc_quality = p.min_resc_quality

@@ -339,21 +339,29 @@ FORAGE = dict(workload="collective_foraging", n_agents=100, radius=10.0, arena=[
               step="resource interaction + social VPF + decision/motion update (3 launches)")
 
 
-def forage_params():
+# the same arena with agent-agent collisions on (AGENT_AGENT_COLLISION=1, ghost mode on)
+FORAGE_COLLIDE = dict(FORAGE, workload="collective_foraging_collisions", steps=2000,
+                      collide_agents=True, ghost_mode=True,
+                      step="agent-agent collisions + resource interaction + social VPF + "
+                           "decision/motion update (4 launches)")
+
+
+def forage_params(collide=False):
     from abm_gb300.foraging import ForageParams
     return ForageParams(width=1000.0, height=1000.0, agent_radius=10.0, patch_radius=30.0,
                         min_resc_units=1000, max_resc_units=1001, min_resc_quality=1.0,
                         max_resc_quality=1.0, consumption=1.0, rv=1200, fov=0.5,
                         vision_range=2000.0, visual_exclusion=True, teleport_exploit=False,
-                        pooling_time=0, seed=FORAGE["seed"])
+                        pooling_time=0, seed=FORAGE["seed"], collide_agents=collide,
+                        ghost_mode=True)
 
 
-def forage_leg(torch, steps=FORAGE["steps"], with_cpu=True):
+def forage_leg(torch, steps=FORAGE["steps"], with_cpu=True, collide=False):
     """The foraging workload run for `steps` steps in CUDA graphs of 100 steps; foraging
     efficiency (units per agent per step, data_loader.py:1333-1346) over the run; the oracle
-    step on the host for a bounded sample of steps."""
+    step on the host for a bounded sample of steps.  collide: agent-agent collisions on."""
     from abm_gb300.foraging import ForagingSim, efficiency
-    prm = forage_params()
+    prm = forage_params(collide)
     sim = ForagingSim(prm, n_agents=FORAGE["n_agents"], n_patches=FORAGE["n_patches"],
                       init_seed=FORAGE["seed"])
     chunk = FORAGE["graph_chunk"]
@@ -368,17 +376,21 @@ def forage_leg(torch, steps=FORAGE["steps"], with_cpu=True):
     t = e0.elapsed_time(e1) * 1e-3
     eff = efficiency(c0, sim.collected(), sim.t - t0)
     n = FORAGE["n_agents"]
-    out = {"workload": FORAGE, "value": n * steps / t, "unit": METRIC,
-           "ms_per_step": t / steps * 1e3, "steps": steps, "gpu_launches": 3 * steps,
+    out = {"workload": FORAGE_COLLIDE if collide else FORAGE, "value": n * steps / t,
+           "unit": METRIC, "ms_per_step": t / steps * 1e3, "steps": steps,
+           "gpu_launches": (4 if collide else 3) * steps,
            "efficiency_mean": float(eff.mean()), "efficiency_max": float(eff.max()),
            "diagnostics": {"nonfinite": int(sim.diag[2].item()),
                            "failed_regenerations": int(sim.diag[4].item())}}
+    if collide:
+        out["agents_in_collide_mode_at_end"] = int(np.sum(sim.agents_numpy()["override_mode"]
+                                                          == 4))
     if with_cpu:
         import oracle
         fp, ip, seed = prm.oracle_arrays()
         ag, pt = sim.agents_numpy(), sim.patches_numpy()
         k, t_cpu = 0, 0.0
-        while t_cpu < 10.0 and k < 400:
+        while t_cpu < (5.0 if collide else 10.0) and k < 400:
             a = time.perf_counter()
             ag, pt, _, _ = oracle.forage_step(ag, pt, fp, ip, seed)
             t_cpu += time.perf_counter() - a
@@ -611,6 +623,8 @@ def run_gb300(args, rank, world):
         line["adjoint"] = adjoint_leg(torch)
     if not args.no_forage:
         line["forage"] = forage_leg(torch, with_cpu=not args.no_cpu_baseline)
+        line["forage_collisions"] = forage_leg(torch, steps=FORAGE_COLLIDE["steps"],
+                                               with_cpu=not args.no_cpu_baseline, collide=True)
     if not args.no_batched:
         line["metarunner"] = metarunner_leg(torch)
     if not args.no_cpu_baseline:
@@ -631,9 +645,9 @@ def profile_workload(which: str):
         b = BatchedSweep(vp, sweep_instances(n_instances=B["n_instances"], seed=B["seed"]))
         for _ in range(8):
             b.step()
-    elif which == "forage":
+    elif which in ("forage", "forage_collide"):
         from abm_gb300.foraging import ForagingSim
-        sim = ForagingSim(forage_params(), n_agents=FORAGE["n_agents"],
+        sim = ForagingSim(forage_params(which == "forage_collide"), n_agents=FORAGE["n_agents"],
                           n_patches=FORAGE["n_patches"], init_seed=FORAGE["seed"])
         for _ in range(300):
             sim.step()
@@ -666,7 +680,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-forage", action="store_true")
-    ap.add_argument("--profile-workload", choices=["batched", "forage", "edge"],
+    ap.add_argument("--profile-workload", choices=["batched", "forage", "forage_collide", "edge"],
                     help="run a few eager steps of one leg's workload and exit (for ncu)")
     args = ap.parse_args()
     if args.profile_workload:

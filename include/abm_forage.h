@@ -2,7 +2,15 @@
  * abm_forage.h -- C ABI of the collective-foraging step (libabm_vpf.so).
  *
  * One timestep of the reference's foraging simulation (abm/simulation/sims.py:734-858, the
- * Simulation.start loop body without agent-agent collisions) for one arena on the GPU:
+ * Simulation.start loop body) for one arena on the GPU:
+ *   0. when collide_agents is set, the agent-agent collisions (sims.py:735-784): agents whose
+ *      integer pygame rects overlap (collide_circle, radius + 2) make the proximity manoeuvre
+ *      of Simulation.agent_agent_collision_proximity (sims.py:421-474: the distance-weighted
+ *      projection field of the agents within 2R + 20, a 0.2 rad turn away from the fuller
+ *      half, a stop when the 200 pixels ahead are occupied) once per collision list that
+ *      holds them (none in ghost mode for pairs with an exploiting agent), enter collide mode
+ *      and, when among the collided agents, are notified with -1; agents no longer colliding
+ *      leave collide mode;
  *   1. agent-resource interaction (sims.py:789-858): agents whose centre lies inside a patch
  *      are turned towards its centre (bias_agent_towards_res_center, sims.py:544-552), notified
  *      about it (notify_agent, sims.py:29-42; teleported to its centre when teleport_exploit)
@@ -61,6 +69,9 @@ typedef struct {
     int32_t visual_exclusion, patchwise_exclusion;
     /* random streams (Philox-4x32-10, keyed by seed; counters per agent / patch) */
     uint64_t seed;
+    /* agent-agent collisions (AGENT_AGENT_COLLISION; needs an integer agent_radius) and ghost
+     * mode (GHOST_WHILE_EXPLOIT: exploiting agents neither collide nor are collided with) */
+    int32_t collide_agents, ghost_mode;
 } abm_forage_params;
 
 /* Agent state, n entries per array (device). */
@@ -88,7 +99,8 @@ typedef struct {
  * Default parameters: decision_params.py / movement_params.py defaults and the foraging
  * workload's arena (1000 x 1000, pad 30, agent radius 10, 3 patches of radius 30 with 1000
  * units, consumption 1, pooling_time 0, teleport_exploit 1, regeneration on, Rv 1200, full
- * field of view, vision range 2000, visual exclusion on, patchwise exclusion on).
+ * field of view, vision range 2000, visual exclusion on, patchwise exclusion on, collisions
+ * off, ghost mode on).
  */
 int abm_forage_params_default(abm_forage_params *p);
 

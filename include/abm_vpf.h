@@ -110,6 +110,12 @@ typedef struct abm_agent_overrides {
 #define ABM_DIAG_TIMEOUTS 3          /* bounded waits that gave up */
 #define ABM_DIAG_CAPACITY 4          /* social fields left empty: more obstacles in range than
                                         the kernel's per-agent capacity (4096) */
+#define ABM_DIAG_COLLIDE_FP64 5      /* foraging collisions: proximity-field bearings whose FP32
+                                        angle lay within 4e-6 rad of a decision boundary and
+                                        were taken on the reference's FP64 route */
+#define ABM_DIAG_COLLIDE_REPLAYS 6   /* foraging collisions: manoeuvres whose half / front
+                                        comparison lay within numpy's rounding and was decided
+                                        by replaying numpy's pairwise sums */
 #define ABM_DIAG_COUNT 8
 
 /* ---------------------------------------------------------------- utilities */

@@ -91,6 +91,8 @@ def lib():
                                                      c_int, dp, c_int, c_int, dp]
             L.orc_social_vpf.argtypes = [c_int, c_int, dp, dp, dp, dp, ip, ip, c_d, c_int, c_int,
                                          c_int, c_d, c_d, dp]
+            L.orc_np_mean.argtypes = [dp, ctypes.c_longlong, ctypes.c_longlong]
+            L.orc_np_mean.restype = c_d
             _lib = L
     return _lib
 
@@ -271,6 +273,8 @@ def forage_step(agents, patches, fp, ip, seed, uniforms=None):
     rv = int(ip[7])
     soc = np.zeros((n, rv), np.float64)
     fp = np.ascontiguousarray(fp, np.float64)
+    # arrays without the collision switches (collide_agents, ghost_mode): collisions off
+    ip = np.concatenate([np.asarray(ip, np.int32), np.array([0, 1], np.int32)[len(ip) - 10:]])
     ip = np.ascontiguousarray(ip, np.int32)
     uni = None if uniforms is None else np.ascontiguousarray(uniforms, np.float64)
     ptr = lambda arr: arr.ctypes.data_as(ctypes.c_void_p)
@@ -279,6 +283,12 @@ def forage_step(agents, patches, fp, ip, seed, uniforms=None):
         ptr(fp), ptr(ip), ctypes.c_uint64(int(seed) & 0xFFFFFFFFFFFFFFFF),
         None if uni is None else ptr(uni), ptr(soc))
     return a, p, soc, int(failed)
+
+
+def np_mean(a):
+    """The oracle's restatement of np.mean over a float64 vector (pairwise summation)."""
+    a = np.ascontiguousarray(a, np.float64)
+    return float(lib().orc_np_mean(_dp(a), len(a), 1))
 
 
 def philox4x32(ctr, key):

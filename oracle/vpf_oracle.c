@@ -518,6 +518,41 @@ int orc_vf_step_range(int n, int i0, int i1, const double *x, const double *y, c
     return mismatch;
 }
 
+/* numpy's pairwise summation of float64 (the add reduction's inner loop, numpy
+ * _core/src/umath/loops_utils.h.src: pairwise_sum): below 8 elements a plain loop, up to 128
+ * eight interleaved accumulators combined as ((r0+r1)+(r2+r3))+((r4+r5)+(r6+r7)) followed
+ * by the remainder, above that the two halves split at a multiple of 8.  a[k * stride]. */
+static double np_pairwise_sum(const double *a, long long n, long long stride)
+{
+    if (n < 8) {
+        double res = 0.0;
+        for (long long k = 0; k < n; ++k) res += a[k * stride];
+        return res;
+    }
+    if (n <= 128) {
+        double r[8];
+        for (int j = 0; j < 8; ++j) r[j] = a[j * stride];
+        long long k;
+        for (k = 8; k < n - (n % 8); k += 8)
+            for (int j = 0; j < 8; ++j) r[j] += a[(k + j) * stride];
+        double res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]));
+        for (; k < n; ++k) res += a[k * stride];
+        return res;
+    }
+    long long n2 = n / 2;
+    n2 -= n2 % 8;
+    return np_pairwise_sum(a, n2, stride) + np_pairwise_sum(a + n2 * stride, n - n2, stride);
+}
+
+/* np.mean of a float64 view: (0 + pairwise sum) / n; NaN for an empty view. */
+static double np_mean(const double *a, long long n, long long stride)
+{
+    if (n <= 0) return NAN;
+    return (0.0 + np_pairwise_sum(a, n, stride)) / (double)n;
+}
+
+double orc_np_mean(const double *a, long long n, long long stride) { return np_mean(a, n, stride); }
+
 int orc_num_threads(void)
 {
 #ifdef _OPENMP
@@ -531,17 +566,22 @@ int orc_num_threads(void)
 /* ---------------------------------------------------------------- foraging social channel */
 
 /*
- * Agent.projection_field (agent.py:457-597) with keep_distance_info = False.
+ * Agent.projection_field (agent.py:457-597).
  * obs_xy: n_obs obstacle top-left positions, the first n_social of them social cues and the
  * rest (present only when has_non_social) non-social occluders.  Every obstacle centre uses
  * the focal radius R (agent.py:504-505).  visual_exclusion applies the distance-ordered
- * interval trimming of exlude_V_source_data (agent.py:421-445).  out: Rv values, flipped and
- * FOV-masked like the reference's return value.
+ * interval trimming of exlude_V_source_data (agent.py:421-445).  The surviving social
+ * intervals are filled in the order of rank_V_source_data("vis_angle") (agent.py:599-603: a
+ * stable sort by visual angle, descending); with keep_distance_info the main run of each
+ * interval is set to 1 - distance / vision_range, where `distance` is the loop variable of
+ * the obstacle loop, i.e. the distance of the LAST non-coincident obstacle (agent.py:526,
+ * :584-586), while the wrapped parts are set to 1 (agent.py:576-582).  out: Rv values, flipped
+ * and FOV-masked like the reference's return value.
  */
-void orc_agent_projection_field(int Rv, double fov0, double fov1, double px, double py, double R,
-                                double orientation, int visual_exclusion, int n_obs,
-                                const double *obs_xy, int n_social, int has_non_social,
-                                double *out)
+static void agent_projection_core(int Rv, double fov0, double fov1, double px, double py,
+                                  double R, double orientation, int visual_exclusion, int n_obs,
+                                  const double *obs_xy, int n_social, int has_non_social,
+                                  int keep_distance_info, double vision_range, double *out)
 {
     double *phis = (double *)malloc(sizeof(double) * (size_t)Rv);
     double *raw = (double *)calloc((size_t)Rv, sizeof(double));
@@ -556,6 +596,7 @@ void orc_agent_projection_field(int Rv, double fov0, double fov1, double px, dou
     int *social = (int *)malloc(sizeof(int) * (size_t)cap);
     int *order = (int *)malloc(sizeof(int) * (size_t)cap);
     int m = 0;
+    double last_d = 0.0;
 
     double v1sx = px + R, v1sy = py + R;
     double v1ex = px + (1 + cos(orientation)) * R;
@@ -571,6 +612,7 @@ void orc_agent_projection_field(int Rv, double fov0, double fov1, double px, dou
         double d = sqrt(ddx * ddx + ddy * ddy);
         double va = 2 * atan(R / (1 * d));
         int t = orc_find_nearest(phis, Rv, ca);
+        last_d = d;
         if (fov0 < ca && ca < fov1) {
             double ps = (va / (2 * ORC_PI)) * Rv;
             dist[m] = d;
@@ -608,12 +650,23 @@ void orc_agent_projection_field(int Rv, double fov0, double fov1, double px, dou
             }
         }
     }
-    for (int a = 0; a < m; ++a) {
+    /* fill order: the distance order of the exclusion step (or list order without it), then
+     * a stable descending sort by visual angle */
+    if (!visual_exclusion)
+        for (int a = 0; a < m; ++a) order[a] = a;
+    for (int a = 1; a < m; ++a) {
+        int key = order[a], b = a - 1;
+        while (b >= 0 && vis[order[b]] < vis[key]) { order[b + 1] = order[b]; --b; }
+        order[b + 1] = key;
+    }
+    const double value = keep_distance_info ? 1 - last_d / vision_range : 1.0;
+    for (int q = 0; q < m; ++q) {
+        int a = order[q];
         if (!social[a]) continue;          /* remove_nonsocial_V_source_data */
         long long s = sx[a], e = ex[a];
         if (s < 0) { np_fill(raw, Rv, Rv + s, Rv, 1.0); s = 0; }
         if (e >= Rv) { np_fill(raw, Rv, 0, e - Rv, 1.0); e = Rv - 1; }
-        np_fill(raw, Rv, s, e, 1.0);
+        np_fill(raw, Rv, s, e, value);
     }
     for (int k = 0; k < Rv; ++k) {
         double val = raw[Rv - 1 - k];
@@ -623,6 +676,16 @@ void orc_agent_projection_field(int Rv, double fov0, double fov1, double px, dou
     }
     free(phis); free(raw); free(dist); free(vis); free(ps0); free(pe0); free(sx); free(ex);
     free(social); free(order);
+}
+
+/* Agent.projection_field with keep_distance_info = False (the social channel). */
+void orc_agent_projection_field(int Rv, double fov0, double fov1, double px, double py, double R,
+                                double orientation, int visual_exclusion, int n_obs,
+                                const double *obs_xy, int n_social, int has_non_social,
+                                double *out)
+{
+    agent_projection_core(Rv, fov0, fov1, px, py, R, orientation, visual_exclusion, n_obs,
+                          obs_xy, n_social, has_non_social, 0, 1.0, out);
 }
 
 /*
@@ -683,8 +746,9 @@ void orc_social_vpf(int i, int n, const double *x, const double *y, const double
 
 /* ---------------------------------------------------------------- foraging step
  *
- * One step of the foraging simulation (abm/simulation/sims.py:734-858 without agent-agent
- * collisions; Agent.update, abm/agent/agent.py:213-283), agents updated from one snapshot.
+ * One step of the foraging simulation (abm/simulation/sims.py:734-858, the agent-agent
+ * collisions when collide_agents is set; Agent.update, abm/agent/agent.py:213-283), agents
+ * updated from one snapshot.
  * Positions, orientation and speed are stored as float32 where the GPU step stores them, so
  * the two can be compared exactly; decision variables, collected units and patches are FP64.
  * Random draws: Philox-4x32-10 (Salmon et al., SC 2011) with the GPU step's counters, or the
@@ -694,8 +758,9 @@ void orc_social_vpf(int i, int n, const double *x, const double *y, const double
  *         exp_theta_min exp_theta_max reloc_theta_max exp_stop_ratio width height window_pad
  *         agent_radius consumption min_resc_quality max_resc_quality patch_radius fov0 fov1
  *         vision_range
- * IP[10]: Tau pooling_time teleport_exploit regenerate_patches allow_border_patch_overlap
+ * IP[12]: Tau pooling_time teleport_exploit regenerate_patches allow_border_patch_overlap
  *         min_resc_units max_resc_units rv visual_exclusion patchwise_exclusion
+ *         collide_agents ghost_mode
  */
 enum { M_EXPLORE = 0, M_RELOCATE = 1, M_EXPLOIT = 2, M_POOL = 3, M_COLLIDE = 4, M_NONE = -1 };
 
@@ -801,6 +866,96 @@ static int f_regenerate(int k, int np, double *px, double *py, double *pr, doubl
     return 0;
 }
 
+/* pygame.sprite.collide_circle (pygame's sprite module) on the agents' rects while their
+ * radius is raised by the proximity distance 2 (sims.py:737-751): rect = int(position)
+ * (pygame stores integer rect coordinates; a float assignment truncates), width int(2R), so
+ * the centre is int(position) + int(2R) / 2; collision when the squared centre distance is at
+ * most ((R + 2) + (R + 2))^2. */
+static int f_rects_collide(const float *x, const float *y, double R, int a, int b)
+{
+    long long half = (long long)(2 * R) / 2;
+    long long dx = ((long long)x[a] + half) - ((long long)x[b] + half);
+    long long dy = ((long long)y[a] + half) - ((long long)y[b] + half);
+    double rr = (R + 2) + (R + 2);
+    return (double)(dx * dx + dy * dy) <= rr * rr;
+}
+
+/* Simulation.agent_agent_collision_proximity (sims.py:421-474) for one collided agent b: the
+ * LIDAR-like proximity field of the agents within 2R + 20 of it (Agent.projection_field with
+ * keep_distance_info, full circle), the turn away from the fuller half and the stop when the
+ * 200 pixels ahead are occupied.  th: the FP64 orientations of this phase. */
+static void f_collide_process(ForagerArrays *A, const double *FP, const int *IP, int n, int b,
+                              const int *expl, double *th, double *obs, double *pf)
+{
+    const double R = FP[22];
+    const int Rv = IP[7];
+    if (!expl[b]) { A->ovr[b] = M_COLLIDE; A->mode[b] = M_COLLIDE; }
+    int n_obs = 0;
+    double c1x = (double)A->x[b] + R, c1y = (double)A->y[b] + R;
+    for (int j = 0; j < n; ++j) {
+        if (j == b) continue;
+        double ddx = ((double)A->x[j] + R) - c1x, ddy = ((double)A->y[j] + R) - c1y;
+        if (sqrt(ddx * ddx + ddy * ddy) < 2 * R + 20) {
+            obs[2 * n_obs] = A->x[j];
+            obs[2 * n_obs + 1] = A->y[j];
+            ++n_obs;
+        }
+    }
+    agent_projection_core(Rv, -ORC_PI, ORC_PI, A->x[b], A->y[b], R, th[b], IP[8], n_obs, obs,
+                          n_obs, 0, 1, FP[29], pf);
+    const long long h = Rv / 2;
+    double le = np_mean(pf, h, 1), re = np_mean(pf + h, Rv - h, 1);
+    double D = (le - re > 0) ? 1.0 : (le - re < 0) ? -1.0 : 0.0;   /* np.sign */
+    if (D == 0) D = -1;
+    if (!expl[b]) th[b] -= D * 0.2;
+    long long lo = h - 100, hi = h + 100;                            /* Python slice rules */
+    if (lo < 0) { lo += Rv; if (lo < 0) lo = 0; }
+    if (hi > Rv) hi = Rv;
+    double front = np_mean(pf + lo, hi - lo, 1);
+    if (front > 0) A->v[b] = 0.0f;
+    else if (!expl[b]) A->v[b] = (float)FP[14];
+}
+
+/* The agent-agent interaction block of Simulation.start (sims.py:735-784): pygame's
+ * groupcollide of the agents with themselves (agent order, each agent's list in agent order),
+ * the proximity manoeuvre for every listed agent (skipped in ghost mode when either agent
+ * exploits), then the collided agents' bookkeeping: an agent left in collide mode returns to
+ * explore, a collided one in collide mode is notified with -1. */
+static void f_collide_phase(ForagerArrays *A, const double *FP, const int *IP, int n)
+{
+    const int ghost = IP[11], tele = IP[2];
+    const double R = FP[22];
+    int *expl = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *coll = (int *)calloc((size_t)(n > 0 ? n : 1), sizeof(int));
+    double *th = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    double *obs = (double *)malloc(sizeof(double) * 2 * (size_t)(n > 0 ? n : 1));
+    double *pf = (double *)malloc(sizeof(double) * (size_t)IP[7]);
+    for (int i = 0; i < n; ++i) { expl[i] = A->ovr[i] == M_EXPLOIT; th[i] = A->th[i]; }
+    for (int a = 0; a < n; ++a)
+        for (int b = 0; b < n; ++b) {
+            if (b == a || !f_rects_collide(A->x, A->y, R, a, b)) continue;
+            if (ghost && (expl[b] || expl[a])) continue;
+            f_collide_process(A, FP, IP, n, b, expl, th, obs, pf);
+        }
+    for (int a = 0; a < n; ++a)
+        for (int b = 0; b < n; ++b) {
+            if (b == a || !f_rects_collide(A->x, A->y, R, a, b)) continue;
+            if (tele) {
+                if (!expl[a]) coll[a] = 1;
+                if (!expl[b]) coll[b] = 1;
+            } else if (!ghost || (!expl[a] && !expl[b])) {
+                coll[a] = coll[b] = 1;
+            }
+        }
+    for (int i = 0; i < n; ++i) {
+        A->th[i] = (float)th[i];
+        int cur = f_get_mode(A, FP, i);
+        if (!coll[i] && cur == M_COLLIDE) { A->ovr[i] = M_NONE; A->mode[i] = M_EXPLORE; }
+        if (coll[i] && cur == M_COLLIDE) f_notify(A, IP[0], i, -1, -1);
+    }
+    free(expl); free(coll); free(th); free(obs); free(pf);
+}
+
 int orc_forage_step(int n, float *x, float *y, float *th, float *v, double *w, double *u,
                     double *col, double *colb, int *mode, int *ovr, int *env, int *envb,
                     int *pool, int *patch, uint32_t *nov, uint64_t *draws, int np, double *px,
@@ -814,6 +969,8 @@ int orc_forage_step(int n, float *x, float *y, float *th, float *v, double *w, d
     int failed = 0;
     int *patch_of = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
     int *destroyed = (int *)calloc((size_t)(np > 0 ? np : 1), sizeof(int));
+    /* 0. agent-agent collisions (sims.py:735-784), when enabled */
+    if (IP[10]) f_collide_phase(&A, FP, IP, n);
     /* 1. agent-resource interaction (sims.py:789-846) */
     for (int i = 0; i < n; ++i) {
         double cx = (double)x[i] + R, cy = (double)y[i] + R;

@@ -105,8 +105,11 @@ def make_case(rng, case):
     return p, ag, pt, uniforms
 
 
-def reference_step(p, ag, pt, uniforms, Agent, Rescource, sims, supcalc):
-    """The reference step for one case; returns (agents dict, patches dict, soc fields)."""
+def reference_step(p, ag, pt, uniforms, Agent, Rescource, sims, supcalc,
+                   before_interaction=None):
+    """The reference step for one case; returns (agents dict, patches dict, soc fields).
+    before_interaction(agents), when given, runs on the reference agents before the
+    agent-resource interaction (the agent-agent collision block of sims.py:735-784)."""
     from abm.contrib import movement_params
     movement_params.exp_theta_min, movement_params.exp_theta_max = (p.exp_theta_min,
                                                                     p.exp_theta_max)
@@ -163,6 +166,8 @@ def reference_step(p, ag, pt, uniforms, Agent, Rescource, sims, supcalc):
         r.resc_left = float(pt["left"][k])
         r.unit_per_timestep = float(pt["quality"][k])
         rescs.append(r)
+    if before_interaction is not None:
+        before_interaction(agents)
     # ---- agent-resource interaction, sims.py:789-855 (refine_ar_overlap_group, sims.py:45-56,
     #      selects the agents whose centre is inside a patch; pygame's circle test before it
     #      accepts a superset of them)

@@ -92,3 +92,85 @@ def test_forage_params_from_env_and_round_trip():
     c = p.to_c()
     assert c.fov0 == -0.5 * math.pi and c.fov1 == 0.5 * math.pi and c.seed == 3
     assert c.min_resc_units == 100 and c.max_resc_units == 101 and c.T_w == 0.4
+    env.update({"AGENT_AGENT_COLLISION": "1", "GHOST_WHILE_EXPLOIT": "0"})
+    q = ForageParams.from_env(env)
+    assert q.collide_agents and not q.ghost_mode
+    fp, ip, seed = q.oracle_arrays()
+    assert len(ip) == 12 and ip[10] == 1 and ip[11] == 0
+    assert ForageParams.from_arrays(fp, ip, seed) == q
+    # arrays written before the collision switches existed: collisions off
+    assert not ForageParams.from_arrays(fp, ip[:10], seed).collide_agents
+
+
+def test_forage_params_struct_layout():
+    """The ctypes mirror of abm_forage_params has the C layout: the library's defaults land in
+    the right fields, up to the last one, and equal ForageParams' defaults."""
+    import ctypes
+    from abm_gb300 import _lib
+    from abm_gb300.foraging import ForageParams
+    lib = _lib.load()
+    c = _lib.AbmForageParams()
+    ctypes.memset(ctypes.byref(c), 0x7F, ctypes.sizeof(c))
+    assert lib.abm_forage_params_default(ctypes.byref(c)) == 0
+    d = ForageParams().to_c()
+    for name, _ in _lib.AbmForageParams._fields_:
+        assert getattr(c, name) == getattr(d, name), name
+    assert (c.rv, c.seed, c.collide_agents, c.ghost_mode) == (1200, 0, 0, 1)
+
+
+def test_np_mean_restatement_matches_numpy():
+    """The oracle's pairwise-summation mean equals np.mean bit for bit, on random vectors and
+    on the proximity fields' value patterns (0, 1 and one weight) seen through flipped views."""
+    rng = np.random.default_rng(11)
+    for _ in range(300):
+        n = int(rng.integers(1, 5000))
+        a = rng.standard_normal(n) * np.exp(rng.uniform(-30, 30, n))
+        assert oracle.np_mean(a) == np.mean(a)
+        w = 1 - rng.uniform(0, 45) / rng.choice([30.0, 150.0, 2000.0])
+        f = np.flip(rng.choice([0.0, 1.0, w], n, p=[0.6, 0.1, 0.3]))
+        h = n // 2
+        for v in (f[:h], f[h:]):
+            if len(v):
+                assert oracle.np_mean(np.ascontiguousarray(v)) == np.mean(v)
+
+
+def test_collision_oracle_matches_reference():
+    """Foraging steps with agent-agent collisions: the oracle against the reference's own
+    collision block (Simulation.agent_agent_collision_proximity with Agent.projection_field
+    and the collided-agent bookkeeping of sims.py:735-784) followed by its step."""
+    cases = load_cases("collision")
+    assert len(cases) >= 16
+    for ci, c in enumerate(cases):
+        assert int(c["ip"][10]) == 1
+        ag = {k[3:]: v for k, v in c.items() if k.startswith("in_")}
+        pt = {k[4:]: v for k, v in c.items() if k.startswith("pin_")}
+        a, p, soc, failed = oracle.forage_step(ag, pt, c["fp"], c["ip"], 0, c["uniforms"])
+        rv = int(c["ip"][7])
+        assert np.array_equal(soc.astype(np.uint8), np.unpackbits(c["soc"], axis=1)[:, :rv]), ci
+        for k in AGENT_INT:
+            assert np.array_equal(a[k].astype(np.int64), c["out_" + k]), (ci, k)
+        for k in ("w", "u", "collected", "collected_before"):
+            np.testing.assert_allclose(a[k], c["out_" + k], rtol=0, atol=1e-12,
+                                       err_msg=f"case {ci} {k}")
+        for k in ("x", "y", "theta", "v"):
+            assert np.max(_ulps32(a[k], c["out_" + k])) <= 2.0, (ci, k)
+        assert np.array_equal(p["left"], c["pout_left"]), ci
+
+
+def test_collision_fixtures_cover_the_branches():
+    """The collision fixtures reach: agents left in collide mode, collide mode ended, stopped
+    agents (front occupied), both ghost settings, both teleport settings, odd and small Rv
+    (front slice from a negative start), a vision range below the proximity radius (negative
+    field weight), and several manoeuvres of one agent in a step."""
+    cases = load_cases("collision")
+    ip = np.array([c["ip"] for c in cases])
+    assert set(ip[:, 11]) == {0, 1} and set(ip[:, 2]) == {0, 1}
+    assert {120, 121} <= set(ip[:, 7].tolist())
+    assert any(float(c["fp"][29]) < 40 for c in cases)
+    out_mode = np.concatenate([c["out_override_mode"] for c in cases])
+    in_mode = np.concatenate([c["in_override_mode"] for c in cases])
+    assert np.sum(out_mode == 4) >= 20
+    assert np.sum((in_mode == 4) & (out_mode != 4)) >= 5
+    stopped = np.concatenate([(c["out_override_mode"] == 4) & (c["out_v"] == 0) for c in cases])
+    assert stopped.sum() >= 5
+    assert sum(int(c["pairs"]) for c in cases) >= 200

@@ -36,9 +36,12 @@ def _check(a, p, soc, want_a, want_p, want_soc, tag):
                                   np.asarray(want_p[k]).astype(np.int64)), (tag, k)
 
 
-def test_forage_step_matches_reference_fixtures():
+@pytest.mark.parametrize("fixture", ["forage", "collision"])
+def test_forage_step_matches_reference_fixtures(fixture):
+    """One step from each fixture state against the reference's own step (the collision
+    fixtures run its agent-agent block first)."""
     from abm_gb300.foraging import ForageParams, ForagingSim
-    for ci, c in enumerate(load_cases("forage")):
+    for ci, c in enumerate(load_cases(fixture)):
         prm = ForageParams.from_arrays(c["fp"], c["ip"], 0)
         ag = {k[3:]: v for k, v in c.items() if k.startswith("in_")}
         pt = {k[4:]: v for k, v in c.items() if k.startswith("pin_")}
@@ -77,10 +80,34 @@ def test_forage_step_matches_oracle_every_step(seed, teleport, pooling):
         assert sim.collected().sum() == 0
 
 
-def test_forage_graph_replay_and_determinism():
+@pytest.mark.parametrize("seed,ghost,teleport,rv", [(21, True, True, 400), (22, False, True, 121),
+                                                    (23, True, False, 1200),
+                                                    (24, False, False, 120)])
+def test_collision_step_matches_oracle_every_step(seed, ghost, teleport, rv):
+    """A crowded arena with agent-agent collisions (60 agents on 250 x 250): 80 steps, each
+    compared with the oracle step from the same state."""
+    from abm_gb300.foraging import ForageParams, ForagingSim
+    prm = ForageParams(seed=seed, width=250.0, height=250.0, rv=rv, min_resc_units=5,
+                       max_resc_units=30, teleport_exploit=teleport, vision_range=200.0,
+                       collide_agents=True, ghost_mode=ghost)
+    sim = ForagingSim(prm, n_agents=60, n_patches=3, init_seed=seed)
+    fp, ip, s = prm.oracle_arrays()
+    collided = 0
+    for t in range(80):
+        a0, p0 = sim.agents_numpy(), sim.patches_numpy()
+        sim.step()
+        a1, p1, soc, failed = oracle.forage_step(a0, p0, fp, ip, s)
+        _check(sim.agents_numpy(), sim.patches_numpy(), sim.soc_numpy(), a1, p1,
+               soc.astype(np.uint8), f"step {t}")
+        collided += int(np.sum(a1["override_mode"] == 4))
+    assert collided >= 40
+
+
+@pytest.mark.parametrize("collide", [False, True])
+def test_forage_graph_replay_and_determinism(collide):
     """A 100-step graph replay gives the eager steps' state; the same seed gives the same run."""
     from abm_gb300.foraging import ForageParams, ForagingSim
-    prm = ForageParams(seed=9, min_resc_units=20, max_resc_units=60)
+    prm = ForageParams(seed=9, min_resc_units=20, max_resc_units=60, collide_agents=collide)
     a = ForagingSim(prm, n_agents=100, n_patches=3, init_seed=2)
     b = ForagingSim(prm, n_agents=100, n_patches=3, init_seed=2)
     for _ in range(200):
@@ -160,3 +187,45 @@ def test_forage_recording_matches_states_and_graph_replay():
     assert len(ag) == 40 and len(ag["0"]["posx"]) == 200 and ag["7"]["agent_name"] == "agent-07"
     assert all(len(v["vfield_up"]) == len(v["vfield_down"]) == 200 for v in ag.values())
     assert len(rs) >= 3 and env["N"] == "40"
+
+
+@pytest.mark.parametrize("rv", [1200, 1201, 400])
+def test_collision_exact_paths_match_oracle(rv):
+    """Mirror-symmetric neighbours (equal pixel counts in the two halves: the half comparison
+    is a tie that numpy's rounding decides) and neighbours exactly ahead or behind (bearings on
+    the field's limits): the kernel takes its exact routes (pairwise-sum replay, FP64
+    bearings; counted in the diagnostics) and still equals the oracle."""
+    from abm_gb300.foraging import ForageParams, ForagingSim, initial_state
+    prm = ForageParams(width=1000.0, height=1000.0, rv=rv, fov=1.0, teleport_exploit=False,
+                       collide_agents=True, ghost_mode=True, vision_range=2000.0, seed=4)
+    scenes = []
+    offsets = [(15, 10), (12, 14), (20, 6), (9, 16), (17, 3), (22, 9)]
+    for k in range(24):
+        a, b = offsets[k % len(offsets)]
+        extra = [(a + 3, 0)] if k % 3 == 0 else ([(-(a + 2), 0)] if k % 3 == 1 else [])
+        scenes.append([(0, 0), (a, -b), (a, b)] + extra)
+    x, y = [], []
+    for k, sc in enumerate(scenes):
+        cx, cy = 80 + 140 * (k % 6), 80 + 140 * (k // 6)
+        for dx, dy in sc:
+            x.append(cx + dx)
+            y.append(cy + dy)
+    n = len(x)
+    ag, pt = initial_state(prm, n, 1, seed=1)
+    ag["x"][:] = np.array(x, np.float32)
+    ag["y"][:] = np.array(y, np.float32)
+    ag["theta"][:] = 0.0
+    ag["override_mode"][:] = -1
+    pt["x"][:], pt["y"][:] = 930.0, 930.0
+    sim = ForagingSim(prm, agents=ag, patches=pt)
+    a0, p0 = sim.agents_numpy(), sim.patches_numpy()
+    sim.step()
+    fp, ip, s = prm.oracle_arrays()
+    a1, p1, soc, failed = oracle.forage_step(a0, p0, fp, ip, s)
+    _check(sim.agents_numpy(), sim.patches_numpy(), sim.soc_numpy(), a1, p1,
+           soc.astype(np.uint8), f"rv {rv}")
+    diag = sim.diag.cpu().numpy()
+    assert int(np.sum(a1["override_mode"] == 4)) >= 40
+    assert diag[5] >= 8, diag        # FP64 bearings (neighbours exactly ahead / behind)
+    if rv % 2 == 0:
+        assert diag[6] >= 4, diag    # pairwise-sum replays (mirror ties)
