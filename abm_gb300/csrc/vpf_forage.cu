@@ -232,66 +232,171 @@ __device__ bool regenerate(const ForageArgs &a, int k) {
     return false;
 }
 
-constexpr int kResourceThreads = 1024;
+constexpr int kResourceThreads = 256;
+// Arenas up to these sizes are staged in shared memory for the resource kernel: its phases are
+// chains of dependent accesses (membership, each patch's sequential loop, notifications), and
+// shared memory turns each global round trip of such a chain into a few cycles.
+constexpr int kStageAgents = 2048, kStagePatches = 256;
+
+static size_t resource_smem_bytes(int n, int np) {
+    return (size_t)64 * n + (size_t)64 * np + 64;
+}
+
+// The agent / patch arrays the resource phases touch, copied into shared memory: `s` gets the
+// shared copies in place of the global ones.
+__device__ void stage_in(const ForageArgs &a, ForageArgs &s, unsigned char *sm) {
+    const int n = a.n, np = a.np, tid = threadIdx.x, nt = blockDim.x;
+    double *w = reinterpret_cast<double *>(sm), *col = w + n, *colb = col + n;
+    double *px = colb + n, *py = px + np, *pr = py + np, *pu = pr + np, *pl = pu + np,
+           *pq = pl + np;
+    uint64_t *pdr = reinterpret_cast<uint64_t *>(pq + np);
+    float *x = reinterpret_cast<float *>(pdr + np), *y = x + n, *th = y + n;
+    int *ovr = reinterpret_cast<int *>(th + n), *env = ovr + n, *envb = env + n,
+        *pool = envb + n, *pid = pool + n, *pof = pid + n, *ptid = pof + n;
+    uint32_t *nov = reinterpret_cast<uint32_t *>(ptid + np);
+    for (int i = tid; i < n; i += nt) {
+        w[i] = a.ag.w[i];
+        col[i] = a.ag.collected[i];
+        colb[i] = a.ag.collected_before[i];
+        x[i] = a.ag.x[i];
+        y[i] = a.ag.y[i];
+        th[i] = a.ag.theta[i];
+        ovr[i] = a.ag.override_mode[i];
+        env[i] = a.ag.env_status[i];
+        envb[i] = a.ag.env_status_before[i];
+        pool[i] = a.ag.pool_success[i];
+        pid[i] = a.ag.patch_id[i];
+        nov[i] = a.ag.novelty[i];
+    }
+    for (int k = tid; k < np; k += nt) {
+        px[k] = a.pt.x[k];
+        py[k] = a.pt.y[k];
+        pr[k] = a.pt.radius[k];
+        pu[k] = a.pt.units[k];
+        pl[k] = a.pt.left[k];
+        pq[k] = a.pt.quality[k];
+        pdr[k] = a.pt.draws[k];
+        ptid[k] = a.pt.id[k];
+    }
+    s.ag.w = w;
+    s.ag.collected = col;
+    s.ag.collected_before = colb;
+    s.ag.x = x;
+    s.ag.y = y;
+    s.ag.theta = th;
+    s.ag.override_mode = ovr;
+    s.ag.env_status = env;
+    s.ag.env_status_before = envb;
+    s.ag.pool_success = pool;
+    s.ag.patch_id = pid;
+    s.ag.novelty = nov;
+    s.patch_of = pof;
+    s.pt.x = px;
+    s.pt.y = py;
+    s.pt.radius = pr;
+    s.pt.units = pu;
+    s.pt.left = pl;
+    s.pt.quality = pq;
+    s.pt.draws = pdr;
+    s.pt.id = ptid;
+}
+
+// Write back what the resource phases may change.
+__device__ void stage_out(const ForageArgs &a, const ForageArgs &s) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int i = tid; i < a.n; i += nt) {
+        a.ag.collected[i] = s.ag.collected[i];
+        a.ag.collected_before[i] = s.ag.collected_before[i];
+        a.ag.x[i] = s.ag.x[i];
+        a.ag.y[i] = s.ag.y[i];
+        a.ag.theta[i] = s.ag.theta[i];
+        a.ag.env_status[i] = s.ag.env_status[i];
+        a.ag.env_status_before[i] = s.ag.env_status_before[i];
+        a.ag.pool_success[i] = s.ag.pool_success[i];
+        a.ag.patch_id[i] = s.ag.patch_id[i];
+        a.ag.novelty[i] = s.ag.novelty[i];
+    }
+    for (int k = tid; k < a.np; k += nt) {
+        a.pt.x[k] = s.pt.x[k];
+        a.pt.y[k] = s.pt.y[k];
+        a.pt.radius[k] = s.pt.radius[k];
+        a.pt.units[k] = s.pt.units[k];
+        a.pt.left[k] = s.pt.left[k];
+        a.pt.quality[k] = s.pt.quality[k];
+        a.pt.draws[k] = s.pt.draws[k];
+        a.pt.id[k] = s.pt.id[k];
+    }
+}
 
 __global__ void __launch_bounds__(kResourceThreads) forage_resource_kernel(ForageArgs a) {
+    extern __shared__ __align__(16) unsigned char rsmem[];
     __shared__ int destroyed[ABM_FORAGE_MAX_PATCHES];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    const double R = a.p.agent_radius;
+    const bool staged = a.n <= kStageAgents && a.np <= kStagePatches;   // block-uniform
+    ForageArgs s = a;
+    if (staged) {
+        stage_in(a, s, rsmem);
+        __syncthreads();
+    }
+    const double R = s.p.agent_radius;
     // 1. the patch holding each agent's centre (refine_ar_overlap_group, sims.py:45-56);
     //    patches never overlap, so there is at most one
-    for (int i = tid; i < a.n; i += blockDim.x) {
-        const double cx = (double)a.ag.x[i] + R, cy = (double)a.ag.y[i] + R;
+    for (int i = tid; i < s.n; i += blockDim.x) {
+        const double cx = (double)s.ag.x[i] + R, cy = (double)s.ag.y[i] + R;
         int hit = -1;
-        for (int k = 0; k < a.np && hit < 0; ++k) {
-            if (a.pt.id[k] < 0) continue;   // a slot whose regeneration failed
+        for (int k = 0; k < s.np && hit < 0; ++k) {
+            if (s.pt.id[k] < 0) continue;   // a slot whose regeneration failed
             // FP32 screen (error far below the one-pixel margin), FP64 test near the edge
-            const float rk = (float)a.pt.radius[k];
-            const float fx = (float)(a.pt.x[k] + a.pt.radius[k]) - (float)cx;
-            const float fy = (float)(a.pt.y[k] + a.pt.radius[k]) - (float)cy;
+            const float rk = (float)s.pt.radius[k];
+            const float fx = (float)(s.pt.x[k] + s.pt.radius[k]) - (float)cx;
+            const float fy = (float)(s.pt.y[k] + s.pt.radius[k]) - (float)cy;
             const float f2 = fx * fx + fy * fy;
             if (f2 > (rk + 1.f) * (rk + 1.f)) continue;
             if (f2 < (rk - 1.f) * (rk - 1.f) && rk > 1.f) {
                 hit = k;
                 continue;
             }
-            const double dx = (a.pt.x[k] + a.pt.radius[k]) - cx;
-            const double dy = (a.pt.y[k] + a.pt.radius[k]) - cy;
-            if (sqrt(dx * dx + dy * dy) < a.pt.radius[k]) hit = k;
+            const double dx = (s.pt.x[k] + s.pt.radius[k]) - cx;
+            const double dy = (s.pt.y[k] + s.pt.radius[k]) - cy;
+            if (sqrt(dx * dx + dy * dy) < s.pt.radius[k]) hit = k;
         }
-        a.patch_of[i] = hit;
+        s.patch_of[i] = hit;
     }
-    for (int k = tid; k < a.np; k += blockDim.x) destroyed[k] = 0;
+    for (int k = tid; k < s.np; k += blockDim.x) destroyed[k] = 0;
     __syncthreads();
     // 2. each patch's agents in agent order (one warp per patch: the loop is sequential)
-    for (int k = warp; k < a.np; k += nw) {
-        if (a.pt.id[k] < 0) continue;   // warp-uniform
+    for (int k = warp; k < s.np; k += nw) {
+        if (s.pt.id[k] < 0) continue;   // warp-uniform
         bool d = false;
-        patch_loop(a, k, &d);
+        patch_loop(s, k, &d);
         if (lane == 0) destroyed[k] = d ? 1 : 0;
     }
     __syncthreads();
     // 3. emptied patches are killed and regenerated in patch order (kill_resource)
     if (tid == 0) {
-        for (int k = 0; k < a.np; ++k) {
+        for (int k = 0; k < s.np; ++k) {
             if (!destroyed[k]) continue;
-            if (!a.p.regenerate_patches) {
-                a.pt.id[k] = -1;
+            if (!s.p.regenerate_patches) {
+                s.pt.id[k] = -1;
                 continue;
             }
-            if (!regenerate(a, k)) {
-                a.pt.id[k] = -1;
-                if (a.diag) atomicAdd(&a.diag[ABM_DIAG_CAPACITY], 1ull);
+            if (!regenerate(s, k)) {
+                s.pt.id[k] = -1;
+                if (s.diag) atomicAdd(&s.diag[ABM_DIAG_CAPACITY], 1ull);
             }
         }
     }
     // 4. agents on no patch (sims.py:848-855), and the exploit flags of the social channel
-    for (int i = tid; i < a.n; i += blockDim.x) {
-        if (a.patch_of[i] < 0) {
-            const int m = get_mode(a, i);
-            if (pooling_done(a, i, m) || m == ABM_MODE_EXPLOIT) notify(a, i, -1, -1);
+    for (int i = tid; i < s.n; i += blockDim.x) {
+        if (s.patch_of[i] < 0) {
+            const int m = get_mode(s, i);
+            if (pooling_done(s, i, m) || m == ABM_MODE_EXPLOIT) notify(s, i, -1, -1);
         }
-        a.exploit[i] = a.ag.override_mode[i] == ABM_MODE_EXPLOIT ? 1 : 0;
+        s.exploit[i] = s.ag.override_mode[i] == ABM_MODE_EXPLOIT ? 1 : 0;
+    }
+    if (staged) {
+        __syncthreads();
+        stage_out(a, s);
     }
 }
 
@@ -302,7 +407,7 @@ __device__ inline double prove_orientation(double t) {
     return t;
 }
 
-constexpr int kUpdateWarps = 4;
+constexpr int kUpdateWarps = 1;
 
 // One warp per agent: the lanes count the social field's pixels (coalesced word loads), lane 0
 // applies the update.
@@ -1166,7 +1271,17 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
         forage_collide_kernel<<<n, kCollideBlock, collide_smem_bytes(p->rv, n), s>>>(a);
         if ((st = check_cuda(cudaGetLastError(), "forage_collide_kernel launch"))) return st;
     }
-    forage_resource_kernel<<<1, kResourceThreads, 0, s>>>(a);
+    {
+        const size_t smem = (n <= kStageAgents && n_patches <= kStagePatches)
+                                ? resource_smem_bytes(n, n_patches) : 0;
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(forage_resource_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            attr = true;
+        }
+        forage_resource_kernel<<<1, kResourceThreads, smem, s>>>(a);
+    }
     if ((st = check_cuda(cudaGetLastError(), "forage_resource_kernel launch"))) return st;
     st = abm_vpf_social_fields(agents->x, agents->y, agents->theta, nullptr, p->agent_radius,
                                a.exploit, agents->patch_id, n, p->vision_range,
