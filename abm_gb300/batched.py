@@ -130,9 +130,10 @@ class BatchedSweep:
         if chunk <= 0 or chunk % 2:
             raise ValueError("chunk must be a positive even number")
         self._stream = torch.cuda.Stream(self.device)
-        self._stream.wait_stream(torch.cuda.current_stream(self.device))
         saved = {k: t.clone() for k, t in self._bufs[self._cur].items()}
         saved_pol = None if self._pol is None else (self._pol.clone(), self._pol_step.clone())
+        # the warm-up steps overwrite the state: they start once the copies are taken
+        self._stream.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(self._stream):
             for _ in range(2):     # builds tables / workspace outside the capture
                 self.step(stream=self._stream)

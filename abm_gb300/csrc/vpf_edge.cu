@@ -514,12 +514,8 @@ static int edge_fwd(const S *in, S *out, int32_t n, const abm_vf_params *p, int3
     a.tho = out->theta;
     a.vo = out->v;
     a.terms = terms_dev;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(edge_fwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             150 * 1024);
-        attr = true;
-    }
+    st = allow_dynamic_smem((const void *)edge_fwd_kernel<T>, 200 * 1024, "edge_fwd_kernel smem");
+    if (st) return st;
     edge_fwd_kernel<T><<<n, 32, smem, (cudaStream_t)stream>>>(a);
     return check_cuda(cudaGetLastError(), "edge_fwd_kernel launch");
 }
@@ -550,12 +546,8 @@ static int edge_bwd(const S *in, const S *grad_out, S *grad_in, double *grad_par
         st = check_cuda(cudaMemsetAsync(grads[k], 0, bytes, s), "cudaMemsetAsync(grad_in)");
         if (st) return st;
     }
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(edge_bwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             150 * 1024);
-        attr = true;
-    }
+    st = allow_dynamic_smem((const void *)edge_bwd_kernel<T>, 200 * 1024, "edge_bwd_kernel smem");
+    if (st) return st;
     edge_bwd_kernel<T><<<n, 32, smem, s>>>(a);
     return check_cuda(cudaGetLastError(), "edge_bwd_kernel launch");
 }

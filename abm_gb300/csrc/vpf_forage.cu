@@ -1262,24 +1262,18 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
     a.uniforms = uniforms_dev;
     a.diag = diag_dev;
     if (p->collide_agents) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(forage_collide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 200 * 1024);
-            attr = true;
-        }
+        if ((st = allow_dynamic_smem((const void *)forage_collide_kernel, 200 * 1024,
+                                     "forage_collide_kernel smem")))
+            return st;
         forage_collide_kernel<<<n, kCollideBlock, collide_smem_bytes(p->rv, n), s>>>(a);
         if ((st = check_cuda(cudaGetLastError(), "forage_collide_kernel launch"))) return st;
     }
     {
         const size_t smem = (n <= kStageAgents && n_patches <= kStagePatches)
                                 ? resource_smem_bytes(n, n_patches) : 0;
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(forage_resource_kernel,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            attr = true;
-        }
+        if ((st = allow_dynamic_smem((const void *)forage_resource_kernel, 200 * 1024,
+                                     "forage_resource_kernel smem")))
+            return st;
         forage_resource_kernel<<<1, kResourceThreads, smem, s>>>(a);
     }
     if ((st = check_cuda(cudaGetLastError(), "forage_resource_kernel launch"))) return st;

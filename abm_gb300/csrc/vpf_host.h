@@ -10,6 +10,9 @@ namespace abm {
 
 int set_error(int code, const char *fmt, ...);
 int check_cuda(cudaError_t e, const char *what);
+// Raise a kernel's dynamic shared-memory limit to `bytes` on the current device, once per
+// (device, kernel).
+int allow_dynamic_smem(const void *func, int bytes, const char *what);
 
 // Host copies of one grid's tables (built in FP64 / long double).
 struct GridHostTables {

@@ -46,6 +46,13 @@ __device__ __forceinline__ int bearing_side(dfl P, dfl Q, dfl c, dfl s) {
     return -df_sign(df_add(df_mul(c, P), df_mul(s, Q)));
 }
 
+// Unsigned key ordered like the float (negative values below positive ones, -0 as +0, NaN
+// above +inf).
+__device__ __forceinline__ unsigned float_order_key(float v) {
+    const unsigned b = __float_as_uint(v + 0.0f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
 // numpy slice a[lo:hi] = 1 on the raw bitmask (negative indices count from the end).
 __device__ __forceinline__ void np_slice_fill(uint32_t *vb, int rv, int lo, int hi) {
     if (lo < 0) { lo += rv; if (lo < 0) lo = 0; }
@@ -208,13 +215,15 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
     int m = over ? 0 : s_count;   // more obstacles than the capacity: reported, field empty
 
     // ---- stable ascending rank by exact squared distance (ties keep the list order): one
-    // entry per thread, every other entry read at the same address by the whole block
+    // entry per thread, every other entry read at the same address by the whole block.  The
+    // key compares as (hi, lo) bit patterns mapped to order-preserving unsigned integers, a
+    // total order even for non-finite input, so the ranks are always a permutation.
     for (int e = tid; e < m; e += nthr) {
-        const float kh = ent[e].dkh, kl = ent[e].dkl;
+        const unsigned kh = float_order_key(ent[e].dkh), kl = float_order_key(ent[e].dkl);
         const int ko = ent[e].ord;
         int rank = 0;
         for (int q = 0; q < m; ++q) {
-            const float oh = ent[q].dkh, ol = ent[q].dkl;
+            const unsigned oh = float_order_key(ent[q].dkh), ol = float_order_key(ent[q].dkl);
             const int oo = ent[q].ord;
             rank += (oh < kh) || (oh == kh && ol < kl) || (oh == kh && ol == kl && oo < ko);
         }
@@ -230,7 +239,10 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
         if (a.visual_exclusion) {
             for (int q = 0; q < r; ++q) {
                 const SocialEntry I = ent[sidx[q]];
-                if (!((I.dkh < F.dkh) || (I.dkh == F.dkh && I.dkl < F.dkl))) continue;
+                const unsigned ih = float_order_key(I.dkh), fh = float_order_key(F.dkh);
+                if (!((ih < fh) ||
+                      (ih == fh && float_order_key(I.dkl) < float_order_key(F.dkl))))
+                    continue;
                 if (sx <= I.s0 && I.s0 <= ex) ex = I.s0;
                 if (sx <= I.e0 && I.e0 <= ex) sx = I.e0;
                 if (I.s0 <= sx && I.e0 >= ex) {
@@ -354,12 +366,9 @@ extern "C" int abm_vpf_social_fields(const float *x_dev, const float *y_dev,
     a.diag = diag_dev;
     a.g = *g;
     const size_t smem = social_smem_bytes(g->words, a.cap);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(vpf_social_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             200 * 1024);
-        attr = true;
-    }
+    if ((st = allow_dynamic_smem((const void *)vpf_social_kernel, 200 * 1024,
+                                 "vpf_social_kernel smem")))
+        return st;
     vpf_social_kernel<<<n, 32 * kSocialWarps, smem, (cudaStream_t)stream>>>(a);
     return check_cuda(cudaGetLastError(), "vpf_social_kernel launch");
 }

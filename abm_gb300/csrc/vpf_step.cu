@@ -851,11 +851,8 @@ static int launch_l1(StepArgs a, int wpa, int split, cudaStream_t stream, int *c
 template <bool TORUS, bool HETERO, bool TMA>
 static int launch_tiled(const StepArgs &a, int warps, cudaStream_t stream) {
     auto kern = vpf_pairs_tiled_kernel<TORUS, HETERO, TMA>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
+    int st = allow_dynamic_smem((const void *)kern, 200 * 1024, "vpf_pairs_tiled_kernel smem");
+    if (st) return st;
     const size_t smem = tiled_smem_bytes(warps, a.tile, a.g.words, HETERO,
                                          tile_buffers(a.n, a.tile));
     const int blocks = (a.n + warps - 1) / warps;

@@ -32,6 +32,21 @@ int check_cuda(cudaError_t e, const char *what) {
     return set_error(ABM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+int allow_dynamic_smem(const void *func, int bytes, const char *what) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, int> done;   // (device, kernel) -> bytes
+    int dev = 0;
+    int st = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (st) return st;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = done.find({dev, func});
+    if (it != done.end() && it->second >= bytes) return ABM_OK;
+    st = check_cuda(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+                    what);
+    if (!st) done[{dev, func}] = bytes;
+    return st;
+}
+
 // np.linspace(-pi, pi, n) (numpy 2.x: arange(n) * step + start, last element = stop).
 void np_linspace_pi(int n, std::vector<double> &out) {
     out.resize(n);

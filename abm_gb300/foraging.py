@@ -335,6 +335,7 @@ class ForagingSim:
                                      for k, c in _lib.FORAGER_FIELDS])
         p_s = _lib.AbmPatchState(*[ctypes.cast(pt[k].data_ptr(), c) for k, c in _lib.PATCH_FIELDS])
         soc, scr = torch.empty_like(self.soc_bits), torch.empty_like(self.scratch)
+        stream.wait_stream(torch.cuda.current_stream(self.device))   # the copies are ready
         _lib.check(self.lib.abm_forage_step(
             ctypes.byref(a_s), self.n, ctypes.byref(p_s), self.np, ctypes.byref(self._cparams),
             _lib.u32ptr(soc), _lib.i32ptr(scr), None, None, ctypes.c_void_p(stream.cuda_stream)),
@@ -344,8 +345,8 @@ class ForagingSim:
     def capture(self, chunk: int = 100):
         """Capture `chunk` steps as a CUDA graph on a private stream."""
         self._stream = torch.cuda.Stream(self.device)
-        self._stream.wait_stream(torch.cuda.current_stream(self.device))
         self._warmup(self._stream)
+        self._stream.wait_stream(torch.cuda.current_stream(self.device))
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, stream=self._stream):
             for _ in range(chunk):
