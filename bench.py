@@ -175,10 +175,21 @@ def cpu_baseline(state, budget_cpu_s=20.0):
     t0 = time.perf_counter()
     oracle.vf_step_range(state, p, 0, n_sample)
     wall = time.perf_counter() - t0
+    # the same restatement on one core, on a smaller sample (about two seconds)
+    n1 = int(max(1, min(n_sample, 2.0 / max(per_agent_cpu, 1e-6))))
+    oracle.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        oracle.vf_step_range(state, p, 0, n1)
+        wall1 = time.perf_counter() - t0
+    finally:
+        oracle.set_threads(threads)
     return {"value": n_sample / wall, "unit": METRIC, "cores": threads, "kind": "port",
             "sample": f"{n_sample} focal agents x 1 step of the N=4096 snapshot "
                       f"({wall:.1f} s wall), FP64 C restatement with OpenMP",
-            "host_cpus": os.cpu_count()}
+            "host_cpus": os.cpu_count(),
+            "one_core": {"value": n1 / wall1, "unit": METRIC,
+                         "sample": f"{n1} focal agents x 1 step, one thread ({wall1:.1f} s)"}}
 
 
 def run_reference(args, rank, world):

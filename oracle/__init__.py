@@ -87,6 +87,7 @@ def lib():
                                             dp, dp]
             L.orc_vf_step_range.restype = c_int
             L.orc_num_threads.restype = c_int
+            L.orc_set_threads.argtypes = [c_int]
             L.orc_agent_projection_field.argtypes = [c_int, c_d, c_d, c_d, c_d, c_d, c_d, c_int,
                                                      c_int, dp, c_int, c_int, dp]
             L.orc_social_vpf.argtypes = [c_int, c_int, dp, dp, dp, dp, ip, ip, c_d, c_int, c_int,
@@ -219,6 +220,11 @@ def vf_step_range(state, params, i0, i1, radii=None):
 
 def num_threads() -> int:
     return int(lib().orc_num_threads())
+
+
+def set_threads(n: int) -> None:
+    """Threads of the oracle's OpenMP loops from now on."""
+    lib().orc_set_threads(int(n))
 
 
 def agent_projection_field(rv, fov, position, radius, orientation, visual_exclusion,

@@ -563,6 +563,17 @@ int orc_num_threads(void)
 #endif
 }
 
+/* Threads of the OpenMP loops from now on (for timing on one core). */
+void orc_set_threads(int n)
+{
+#ifdef _OPENMP
+    extern void omp_set_num_threads(int);
+    omp_set_num_threads(n > 0 ? n : 1);
+#else
+    (void)n;
+#endif
+}
+
 /* ---------------------------------------------------------------- foraging social channel */
 
 /*
