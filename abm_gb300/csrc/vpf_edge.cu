@@ -101,23 +101,28 @@ __device__ __forceinline__ void edge_geometry(T dx, T dy, T th, T R, int use_asi
     else a = m_atan(R / d);
 }
 
-// Builds the merged arcs of focal agent i in the warp's shared memory.
+constexpr int kEdgeWarps = 4;   // warps per focal agent
+
+template <typename T>
+__device__ int edge_merge(unsigned char *smem, const EdgeSmem &L, int P, int lane, T kTwoPi,
+                          const Arcs<T> &r);
+
+// Builds the merged arcs of focal agent i in the block's shared memory: the intervals and
+// their sort use every thread of the block, the scans over the sorted intervals warp 0.  The
+// result is valid in every thread.
 template <typename T>
 __device__ Arcs<T> edge_arcs(const EdgeArgs<T> &p, int i, unsigned char *smem) {
-    const int lane = threadIdx.x & 31;
+    __shared__ int s_count;
+    const int tid = threadIdx.x, lane = tid & 31, nthr = blockDim.x;
     const EdgeSmem L = edge_smem<T>(p.cap);
     T *key = reinterpret_cast<T *>(smem + L.key);
     T *up = reinterpret_cast<T *>(smem + L.up);
     int *id = reinterpret_cast<int *>(smem + L.id);
-    T *pm = reinterpret_cast<T *>(smem + L.pm);
-    int *pmi = reinterpret_cast<int *>(smem + L.pmi);
-    EdgeArc<T> *arc = reinterpret_cast<EdgeArc<T> *>(smem + L.arc);
     const T xi = p.x[i], yi = p.y[i], th = p.th[i];
     const T kTwoPi = T(6.283185307179586), kPiT = T(3.141592653589793);
     // intervals (lower end in [-pi, pi), upper = lower + 2a), padded to a power of two
-    int P = 32;
-    while (P < p.n) P <<= 1;
-    for (int j = lane; j < P; j += 32) {
+    const int P = p.cap;
+    for (int j = tid; j < P; j += nthr) {
         T k = Lim<T>::big(), u = -Lim<T>::big();
         int jj = -1;
         if (j < p.n && j != i) {
@@ -136,11 +141,11 @@ __device__ Arcs<T> edge_arcs(const EdgeArgs<T> &p, int i, unsigned char *smem) {
         up[j] = u;
         id[j] = jj;
     }
-    __syncwarp();
+    __syncthreads();
     // bitonic sort by lower end
     for (int size = 2; size <= P; size <<= 1) {
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = lane; t < P / 2; t += 32) {
+            for (int t = tid; t < P / 2; t += nthr) {
                 const int lo = 2 * t - (t & (stride - 1));
                 const int hi = lo + stride;
                 const bool asc = (lo & size) == 0;
@@ -156,9 +161,31 @@ __device__ Arcs<T> edge_arcs(const EdgeArgs<T> &p, int i, unsigned char *smem) {
                     id[hi] = il;
                 }
             }
-            __syncwarp();
+            __syncthreads();
         }
     }
+    Arcs<T> r;
+    r.lo = reinterpret_cast<T *>(smem + L.key);   // reuse key/up/id/pmi as arc arrays
+    r.hi = reinterpret_cast<T *>(smem + L.up);
+    r.lid = reinterpret_cast<int *>(smem + L.id);
+    r.hid = reinterpret_cast<int *>(smem + L.pmi);
+    if (tid < 32) s_count = edge_merge<T>(smem, L, P, lane, kTwoPi, r);
+    __syncthreads();
+    r.count = s_count;
+    return r;
+}
+
+// Warp 0: merges the sorted intervals into arcs (prefix max of the upper ends, arc starts,
+// closing ends, seam fold) and writes them to r; returns their count (-1: the whole circle).
+template <typename T>
+__device__ int edge_merge(unsigned char *smem, const EdgeSmem &L, int P, int lane, T kTwoPi,
+                          const Arcs<T> &r) {
+    T *key = reinterpret_cast<T *>(smem + L.key);
+    T *up = reinterpret_cast<T *>(smem + L.up);
+    int *id = reinterpret_cast<int *>(smem + L.id);
+    T *pm = reinterpret_cast<T *>(smem + L.pm);
+    int *pmi = reinterpret_cast<int *>(smem + L.pmi);
+    EdgeArc<T> *arc = reinterpret_cast<EdgeArc<T> *>(smem + L.arc);
     // prefix max of the upper ends (with the index of the maximiser), chunk per lane
     const int C = P / 32;
     const int c0 = lane * C;
@@ -230,15 +257,7 @@ __device__ Arcs<T> edge_arcs(const EdgeArgs<T> &p, int i, unsigned char *smem) {
         __syncwarp();
     }
     // seam: arcs whose lower end + 2 pi lies under the last arc's upper end fold into it
-    Arcs<T> r;
-    r.lo = reinterpret_cast<T *>(smem + L.key);   // reuse key/up/id/pmi as arc arrays
-    r.hi = reinterpret_cast<T *>(smem + L.up);
-    r.lid = reinterpret_cast<int *>(smem + L.id);
-    r.hid = reinterpret_cast<int *>(smem + L.pmi);
-    if (K == 0) {
-        r.count = 0;
-        return r;
-    }
+    if (K == 0) return 0;
     const EdgeArc<T> last = arc[K - 1];
     const T ulast = last.hi;
     int fold = 0;   // number of leading arcs folded into the last one
@@ -246,10 +265,7 @@ __device__ Arcs<T> edge_arcs(const EdgeArgs<T> &p, int i, unsigned char *smem) {
         if (arc[a].lo + kTwoPi <= ulast) ++fold;
         else break;
     }
-    if (fold >= K) {
-        r.count = -1;   // the whole circle is covered: no edges, zero blob integrals
-        return r;
-    }
+    if (fold >= K) return -1;   // the whole circle is covered: no edges, zero blob integrals
     T new_hi = ulast;
     int new_hid = last.pos;
     if (fold > 0) {
@@ -269,8 +285,7 @@ __device__ Arcs<T> edge_arcs(const EdgeArgs<T> &p, int i, unsigned char *smem) {
         r.hid[a] = (fold + a == K - 1) ? new_hid : A.pos;
     }
     __syncwarp();
-    r.count = cnt;
-    return r;
+    return cnt;
 }
 
 template <typename T>
@@ -365,10 +380,11 @@ __device__ __forceinline__ EdgeUpd<T> edge_update(const EdgeArgs<T> &p, T x, T y
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32) edge_fwd_kernel(const EdgeArgs<T> p) {
+__global__ void __launch_bounds__(32 * kEdgeWarps) edge_fwd_kernel(const EdgeArgs<T> p) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int i = blockIdx.x, lane = threadIdx.x;
     const Arcs<T> A = edge_arcs<T>(p, i, smem);
+    if (threadIdx.x >= 32) return;   // integrals and update: warp 0
     T bc = 0, bs = 0, ec = 0, es = 0;
     if (A.count > 0) edge_integrals<T>(A, bc, bs, ec, es);
     if (lane == 0) {
@@ -393,12 +409,24 @@ __global__ void __launch_bounds__(32) edge_fwd_kernel(const EdgeArgs<T> p) {
 // Adjoint of one step: given d loss / d state(t+1), accumulate d loss / d state(t) and the
 // parameter gradients.  gx0.. must be zero before the launch (contributions are atomics).
 template <typename T>
-__global__ void __launch_bounds__(32) edge_bwd_kernel(const EdgeArgs<T> p) {
+__global__ void __launch_bounds__(32 * kEdgeWarps) edge_bwd_kernel(const EdgeArgs<T> p) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int i = blockIdx.x, lane = threadIdx.x;
+    __shared__ T s_terms[4], s_part[3][kEdgeWarps];
+    const int i = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nthr = blockDim.x;
     const Arcs<T> A = edge_arcs<T>(p, i, smem);
-    T bc = 0, bs = 0, ec = 0, es = 0;
-    if (A.count > 0) edge_integrals<T>(A, bc, bs, ec, es);
+    if (warp == 0) {   // integrals: warp 0, then shared with the block
+        T tb = 0, tbs = 0, te = 0, tes = 0;
+        if (A.count > 0) edge_integrals<T>(A, tb, tbs, te, tes);
+        if (lane == 0) {
+            s_terms[0] = tb;
+            s_terms[1] = tbs;
+            s_terms[2] = te;
+            s_terms[3] = tes;
+        }
+    }
+    __syncthreads();
+    const T bc = s_terms[0], bs = s_terms[1], ec = s_terms[2], es = s_terms[3];
     const T x = p.x[i], y = p.y[i], th = p.th[i], v = p.v[i];
     const T dv = p.gam * (p.v0 - v) + p.alp0 * bc + p.alp0 * p.alp1 * ec;
     const T dpsi = p.bet0 * bs + p.bet0 * p.bet1 * es;
@@ -421,7 +449,7 @@ __global__ void __launch_bounds__(32) edge_bwd_kernel(const EdgeArgs<T> p) {
     // ---- through the arc ends to bearings / half angles, then to positions and heading
     T g_thf = 0, g_xf = 0, g_yf = 0;
     if (A.count > 0) {
-        for (int a = lane; a < 2 * A.count; a += 32) {
+        for (int a = tid; a < 2 * A.count; a += nthr) {
             const int arc = a >> 1;
             const bool upper = a & 1;
             const T e = upper ? A.hi[arc] : A.lo[arc];
@@ -452,6 +480,18 @@ __global__ void __launch_bounds__(32) edge_bwd_kernel(const EdgeArgs<T> p) {
     g_xf = warp_sum(g_xf);
     g_yf = warp_sum(g_yf);
     if (lane == 0) {
+        s_part[0][warp] = g_thf;
+        s_part[1][warp] = g_xf;
+        s_part[2][warp] = g_yf;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        g_thf = g_xf = g_yf = T(0);
+        for (int w = 0; w < nthr / 32; ++w) {   // fixed order
+            g_thf += s_part[0][w];
+            g_xf += s_part[1][w];
+            g_yf += s_part[2][w];
+        }
         atomicAdd(&p.gx0[i], g_x + g_xf);
         atomicAdd(&p.gy0[i], g_y + g_yf);
         atomicAdd(&p.gth0[i], g_th + g_thf);
@@ -516,7 +556,7 @@ static int edge_fwd(const S *in, S *out, int32_t n, const abm_vf_params *p, int3
     a.terms = terms_dev;
     st = allow_dynamic_smem((const void *)edge_fwd_kernel<T>, 200 * 1024, "edge_fwd_kernel smem");
     if (st) return st;
-    edge_fwd_kernel<T><<<n, 32, smem, (cudaStream_t)stream>>>(a);
+    edge_fwd_kernel<T><<<n, 32 * kEdgeWarps, smem, (cudaStream_t)stream>>>(a);
     return check_cuda(cudaGetLastError(), "edge_fwd_kernel launch");
 }
 
@@ -548,7 +588,7 @@ static int edge_bwd(const S *in, const S *grad_out, S *grad_in, double *grad_par
     }
     st = allow_dynamic_smem((const void *)edge_bwd_kernel<T>, 200 * 1024, "edge_bwd_kernel smem");
     if (st) return st;
-    edge_bwd_kernel<T><<<n, 32, smem, s>>>(a);
+    edge_bwd_kernel<T><<<n, 32 * kEdgeWarps, smem, s>>>(a);
     return check_cuda(cudaGetLastError(), "edge_bwd_kernel launch");
 }
 
