@@ -582,9 +582,15 @@ static int edge_bwd(const S *in, const S *grad_out, S *grad_in, double *grad_par
     cudaStream_t s = (cudaStream_t)stream;
     const size_t bytes = sizeof(T) * (size_t)n;
     T *const grads[4] = {a.gx0, a.gy0, a.gth0, a.gv0};
-    for (int k = 0; k < 4; ++k) {
-        st = check_cuda(cudaMemsetAsync(grads[k], 0, bytes, s), "cudaMemsetAsync(grad_in)");
+    if (a.gy0 == a.gx0 + n && a.gth0 == a.gy0 + n && a.gv0 == a.gth0 + n) {
+        // one (4, n) array: one memset
+        st = check_cuda(cudaMemsetAsync(a.gx0, 0, 4 * bytes, s), "cudaMemsetAsync(grad_in)");
         if (st) return st;
+    } else {
+        for (int k = 0; k < 4; ++k) {
+            st = check_cuda(cudaMemsetAsync(grads[k], 0, bytes, s), "cudaMemsetAsync(grad_in)");
+            if (st) return st;
+        }
     }
     st = allow_dynamic_smem((const void *)edge_bwd_kernel<T>, 200 * 1024, "edge_bwd_kernel smem");
     if (st) return st;

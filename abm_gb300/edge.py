@@ -45,6 +45,30 @@ def edge_step(lib, base, pvec, cur, nxt, use_asin, stream, terms=None):
                    ctypes.c_void_p(stream.cuda_stream)), "abm_vpf_edge_fwd")
 
 
+class _Stepper:
+    """One rollout's forward launches with their ctypes arguments built once: parameters,
+    stream, and the state structs of the buffers it steps between."""
+
+    def __init__(self, lib, base, pv, dtype, use_asin, stream):
+        self.fwd, self.bwd, _ = _fns(lib, dtype)
+        self.cp = _cparams(base, pv)
+        self.asin = 1 if use_asin else 0
+        self.stream = ctypes.c_void_p(stream.cuda_stream)
+        self._structs = {}
+
+    def struct(self, bufs):
+        key = tuple(t.data_ptr() for t in bufs)
+        st = self._structs.get(key)
+        if st is None:
+            st = self._structs[key] = _state(bufs)
+        return st
+
+    def step(self, cur, nxt):
+        _lib.check(self.fwd(ctypes.byref(self.struct(cur)), ctypes.byref(self.struct(nxt)),
+                            cur[0].numel(), ctypes.byref(self.cp), self.asin, None, self.stream),
+                   "abm_vpf_edge_fwd")
+
+
 class _EdgeRollout(torch.autograd.Function):
     @staticmethod
     def forward(ctx, pvec, x0, y0, th0, v0, base, steps, checkpoint, use_asin):
@@ -55,11 +79,12 @@ class _EdgeRollout(torch.autograd.Function):
         dtype = torch.float64 if x0.dtype == torch.float64 else torch.float32
         cur = [t.detach().to(dtype).contiguous().clone() for t in (x0, y0, th0, v0)]
         nxt = [torch.empty_like(t) for t in cur]
+        stepper = _Stepper(lib, base, pv, dtype, use_asin, stream)
         ckpts = []
         for k in range(steps):
             if k % checkpoint == 0:
                 ckpts.append([t.clone() for t in cur])
-            edge_step(lib, base, pv, cur, nxt, use_asin, stream)
+            stepper.step(cur, nxt)
             cur, nxt = nxt, cur
         ctx.base, ctx.steps, ctx.checkpoint, ctx.use_asin = base, steps, checkpoint, use_asin
         ctx.pv = pv
@@ -76,28 +101,30 @@ class _EdgeRollout(torch.autograd.Function):
         _, bwd, _ = _fns(lib, dtype)
         stream = torch.cuda.current_stream(dev)
         n = ctx.ckpts[0][0].numel()
-        zeros = lambda t: torch.zeros(n, dtype=dtype, device=dev) if t is None else t
-        g = [zeros(t).to(dtype).contiguous() for t in (gx, gy, gth, gv)]
-        gin = [torch.empty_like(t) for t in g]
+        # gradient buffers as rows of (4, n) arrays: the adjoint clears one in a single memset
+        G = torch.zeros((4, n), dtype=dtype, device=dev)
+        for r, t in enumerate((gx, gy, gth, gv)):
+            if t is not None:
+                G[r].copy_(t)
+        Gin = torch.empty_like(G)
+        g, gin = list(G.unbind(0)), list(Gin.unbind(0))
         gparams = torch.zeros(5, dtype=torch.float64, device=dev)
-        cp = _cparams(base, pv)
+        stepper = _Stepper(lib, base, pv, dtype, use_asin, stream)
+        gp_ptr = _lib.dptr(gparams)
+        # the states of one segment: the checkpoint, then K - 1 recomputed ones (reused)
+        seg_bufs = [[torch.empty_like(t) for t in ctx.ckpts[0]] for _ in range(K - 1)]
         for seg in range(len(ctx.ckpts) - 1, -1, -1):
             t0 = seg * K
             t1 = min(t0 + K, steps)
-            # recompute the segment's states from its checkpoint
-            states = [ctx.ckpts[seg]]
-            cur = [t.clone() for t in ctx.ckpts[seg]]
-            for _ in range(t0, t1 - 1):
-                nxt = [torch.empty_like(t) for t in cur]
-                edge_step(lib, base, pv, cur, nxt, use_asin, stream)
-                states.append(nxt)
-                cur = nxt
+            states = [ctx.ckpts[seg]] + seg_bufs[:t1 - t0 - 1]
+            for k in range(t1 - t0 - 1):   # recompute the segment from its checkpoint
+                stepper.step(states[k], states[k + 1])
             for k in range(t1 - 1, t0 - 1, -1):
-                st = states[k - t0]
                 _lib.check(bwd(
-                    ctypes.byref(_state(st)), ctypes.byref(_state(g)), ctypes.byref(_state(gin)),
-                    _lib.dptr(gparams), n, ctypes.byref(cp), 1 if use_asin else 0,
-                    ctypes.c_void_p(stream.cuda_stream)), "abm_vpf_edge_bwd")
+                    ctypes.byref(stepper.struct(states[k - t0])),
+                    ctypes.byref(stepper.struct(g)), ctypes.byref(stepper.struct(gin)),
+                    gp_ptr, n, ctypes.byref(stepper.cp), stepper.asin, stepper.stream),
+                    "abm_vpf_edge_bwd")
                 g, gin = gin, g
         gp = gparams.to(ctx.pdtype)
         return (gp, g[0].clone(), g[1].clone(), g[2].clone(), g[3].clone(), None, None, None,
