@@ -4,13 +4,14 @@
 //
 // Three launches per step on the caller's stream (four with agent-agent collisions, whose
 // kernel comes first; see the collisions section):
-//  * forage_resource_kernel (one block): which patch (if any) holds each agent's centre; then
+//  * forage_resource_kernel (one block; small arenas staged in shared memory): which patch (if
+//    any) holds each agent's centre; then
 //    one warp per patch replays the reference's per-patch loop in agent order (the loop is
 //    sequential within a patch: depletion order decides who gets the last units); then the
 //    emptied patches are regenerated in patch order and the agents on no patch are notified;
 //  * the social channel (abm_vpf_social_fields) on the resulting positions, modes and patches;
-//  * forage_update_kernel (one thread per agent): private information, decision processes,
-//    mode, random walk / relocation / exploitation stop, move, walls.
+//  * forage_update_kernel (one warp per agent, one agent per block): private information,
+//    decision processes, mode, random walk / relocation / exploitation stop, move, walls.
 // Decision and motion arithmetic is FP64 (the reference's Python floats); positions,
 // orientation and speed are stored as float32, rounded where the step writes them.  Random
 // numbers come from a Philox-4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
