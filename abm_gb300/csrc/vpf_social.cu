@@ -67,9 +67,10 @@ static __host__ __device__ __forceinline__ size_t align16(size_t b) {
 }
 
 // Shared-memory carve-up of vpf_social_kernel: bitmask, entries, sorted index, trimmed
-// intervals, each region starting on a 16-byte boundary.
+// intervals, the entries in rank order (distance keys and untrimmed interval, one 16-byte
+// record each), each region starting on a 16-byte boundary.
 struct SocialSmem {
-    size_t ent, sidx, trim, total;
+    size_t ent, sidx, trim, srt, total;
 };
 
 static __host__ __device__ __forceinline__ SocialSmem social_smem(int words, int cap) {
@@ -77,7 +78,8 @@ static __host__ __device__ __forceinline__ SocialSmem social_smem(int words, int
     l.ent = align16((size_t)words * 4);
     l.sidx = align16(l.ent + (size_t)cap * sizeof(SocialEntry));
     l.trim = align16(l.sidx + (size_t)cap * sizeof(int));
-    l.total = align16(l.trim + (size_t)cap * sizeof(int2));
+    l.srt = align16(l.trim + (size_t)cap * sizeof(int2));
+    l.total = align16(l.srt + (size_t)cap * sizeof(uint4));
     return l;
 }
 
@@ -97,6 +99,7 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
     SocialEntry *ent = reinterpret_cast<SocialEntry *>(smem + L.ent);
     int *sidx = reinterpret_cast<int *>(smem + L.sidx);     // entries by ascending distance
     int2 *trim = reinterpret_cast<int2 *>(smem + L.trim);   // trimmed (start, end) per entry
+    uint4 *srt = reinterpret_cast<uint4 *>(smem + L.srt);   // by rank: key hi, key lo, s0, e0
     for (int w = tid; w < words; w += nthr) vb[w] = 0u;
     if (tid == 0) {
         s_count = 0;
@@ -228,24 +231,23 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
             rank += (oh < kh) || (oh == kh && ol < kl) || (oh == kh && ol == kl && oo < ko);
         }
         sidx[rank] = e;
+        srt[rank] = make_uint4(kh, kl, (unsigned)ent[e].s0, (unsigned)ent[e].e0);
     }
     __syncthreads();
     // ---- trim each interval against the strictly closer ones, in ascending order (one
-    // focal interval per thread)
+    // focal interval per thread; the closer ones read in rank order, one record each)
     for (int r = tid; r < m; r += nthr) {
         const int fe = sidx[r];
-        const SocialEntry F = ent[fe];
-        int sx = F.s0, ex = F.e0;
+        const uint4 F = srt[r];
+        int sx = (int)F.z, ex = (int)F.w;
         if (a.visual_exclusion) {
             for (int q = 0; q < r; ++q) {
-                const SocialEntry I = ent[sidx[q]];
-                const unsigned ih = float_order_key(I.dkh), fh = float_order_key(F.dkh);
-                if (!((ih < fh) ||
-                      (ih == fh && float_order_key(I.dkl) < float_order_key(F.dkl))))
-                    continue;
-                if (sx <= I.s0 && I.s0 <= ex) ex = I.s0;
-                if (sx <= I.e0 && I.e0 <= ex) sx = I.e0;
-                if (I.s0 <= sx && I.e0 >= ex) {
+                const uint4 I = srt[q];
+                if (!((I.x < F.x) || (I.x == F.x && I.y < F.y))) continue;   // strictly closer
+                const int is0 = (int)I.z, ie0 = (int)I.w;
+                if (sx <= is0 && is0 <= ex) ex = is0;
+                if (sx <= ie0 && ie0 <= ex) sx = ie0;
+                if (is0 <= sx && ie0 >= ex) {
                     sx = 0;
                     ex = 0;
                 }
@@ -366,7 +368,7 @@ extern "C" int abm_vpf_social_fields(const float *x_dev, const float *y_dev,
     a.diag = diag_dev;
     a.g = *g;
     const size_t smem = social_smem_bytes(g->words, a.cap);
-    if ((st = allow_dynamic_smem((const void *)vpf_social_kernel, 200 * 1024,
+    if ((st = allow_dynamic_smem((const void *)vpf_social_kernel, (int)smem,
                                  "vpf_social_kernel smem")))
         return st;
     vpf_social_kernel<<<n, 32 * kSocialWarps, smem, (cudaStream_t)stream>>>(a);
