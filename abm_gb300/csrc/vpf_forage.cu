@@ -120,7 +120,7 @@ __device__ inline bool pooling_done(const ForageArgs &a, int i, int m) {
 // (without D, members just take their pooling notification and their want).  The turn
 // towards the patch centre reads only the agent's own position and orientation and comes
 // first for every member.
-__device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed) {
+__device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed, int *mq) {
     const int lane = threadIdx.x & 31;
     const double R = a.p.agent_radius;
     const double pcx = a.pt.x[k] + a.pt.radius[k], pcy = a.pt.y[k] + a.pt.radius[k];
@@ -154,10 +154,10 @@ __device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed) {
     }
     take_D = __shfl_sync(ABM_FULL_MASK, take_D, 0);
     left = __shfl_sync(ABM_FULL_MASK, left, 0);
-    // (2) every member's own sequence
-    for (int base = 0; base < a.n; base += 32) {
-        const int i = base + lane;
-        if (!(i < a.n && a.patch_of[i] == k)) continue;
+    // (2) every member's own sequence.  The members are queued (ballot compaction, order
+    //     free: they are independent given D) and run 32 at a time, so the FP64 turn below is
+    //     issued once per 32 members rather than once per 32 agents.
+    auto member = [&](int i) {
         // bias_agent_towards_res_center (sims.py:544-552)
         const double dx = pcx - ((double)a.ag.x[i] + R), dy = pcy - ((double)a.ag.y[i] + R);
         double cl = fmod(atan2(dy, dx) + (double)a.ag.theta[i], 2.0 * M_PI);
@@ -166,7 +166,7 @@ __device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed) {
         if (i > D) {
             notify(a, i, -1, -1);
             notify(a, i, -1, -1);
-            continue;
+            return;
         }
         const int mode = get_mode(a, i);
         if (pooling_done(a, i, mode)) {
@@ -181,7 +181,23 @@ __device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed) {
             a.ag.collected[i] += i == D ? take_D : want;
         }
         if (D != INT_MAX) notify(a, i, -1, -1);
+    };
+    int qn = 0;   // warp-uniform
+    for (int base = 0; base < a.n; base += 32) {
+        const int i = base + lane;
+        const bool mem = i < a.n && a.patch_of[i] == k;
+        const unsigned mm = __ballot_sync(ABM_FULL_MASK, mem);
+        if (mem) mq[qn + __popc(mm & ((1u << lane) - 1u))] = i;
+        qn += __popc(mm);
+        __syncwarp();
+        if (qn >= 32) {
+            qn -= 32;
+            member(mq[qn + lane]);
+            __syncwarp();
+        }
     }
+    if (lane < qn) member(mq[lane]);
+    __syncwarp();
     if (lane == 0) a.pt.left[k] = left;
     *destroyed = D != INT_MAX;
 }
@@ -332,6 +348,7 @@ __device__ void stage_out(const ForageArgs &a, const ForageArgs &s) {
 __global__ void __launch_bounds__(kResourceThreads) forage_resource_kernel(ForageArgs a) {
     extern __shared__ __align__(16) unsigned char rsmem[];
     __shared__ int destroyed[ABM_FORAGE_MAX_PATCHES];
+    __shared__ int mqueue[kResourceThreads / 32][64];   // per patch warp: queued members
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
     const bool staged = a.n <= kStageAgents && a.np <= kStagePatches;   // block-uniform
     ForageArgs s = a;
@@ -340,17 +357,31 @@ __global__ void __launch_bounds__(kResourceThreads) forage_resource_kernel(Forag
         __syncthreads();
     }
     const double R = s.p.agent_radius;
+    // FP32 centre and radius of each patch, once (the screen below only needs them to far
+    // better than a pixel)
+    __shared__ float3 pcf[kStagePatches];
+    if (staged) {
+        for (int k = tid; k < s.np; k += blockDim.x)
+            pcf[k] = make_float3((float)(s.pt.x[k] + s.pt.radius[k]),
+                                 (float)(s.pt.y[k] + s.pt.radius[k]), (float)s.pt.radius[k]);
+        __syncthreads();
+    }
     // 1. the patch holding each agent's centre (refine_ar_overlap_group, sims.py:45-56);
     //    patches never overlap, so there is at most one
     for (int i = tid; i < s.n; i += blockDim.x) {
         const double cx = (double)s.ag.x[i] + R, cy = (double)s.ag.y[i] + R;
+        const float cxf = (float)cx, cyf = (float)cy;
         int hit = -1;
         for (int k = 0; k < s.np && hit < 0; ++k) {
             if (s.pt.id[k] < 0) continue;   // a slot whose regeneration failed
             // FP32 screen (error far below the one-pixel margin), FP64 test near the edge
-            const float rk = (float)s.pt.radius[k];
-            const float fx = (float)(s.pt.x[k] + s.pt.radius[k]) - (float)cx;
-            const float fy = (float)(s.pt.y[k] + s.pt.radius[k]) - (float)cy;
+            const float3 c = staged ? pcf[k]
+                                    : make_float3((float)(s.pt.x[k] + s.pt.radius[k]),
+                                                  (float)(s.pt.y[k] + s.pt.radius[k]),
+                                                  (float)s.pt.radius[k]);
+            const float rk = c.z;
+            const float fx = c.x - cxf;
+            const float fy = c.y - cyf;
             const float f2 = fx * fx + fy * fy;
             if (f2 > (rk + 1.f) * (rk + 1.f)) continue;
             if (f2 < (rk - 1.f) * (rk - 1.f) && rk > 1.f) {
@@ -369,7 +400,7 @@ __global__ void __launch_bounds__(kResourceThreads) forage_resource_kernel(Forag
     for (int k = warp; k < s.np; k += nw) {
         if (s.pt.id[k] < 0) continue;   // warp-uniform
         bool d = false;
-        patch_loop(s, k, &d);
+        patch_loop(s, k, &d, mqueue[warp]);
         if (lane == 0) destroyed[k] = d ? 1 : 0;
     }
     __syncthreads();
