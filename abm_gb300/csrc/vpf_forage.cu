@@ -12,8 +12,9 @@
 //  * the social channel (abm_vpf_social_fields) on the resulting positions, modes and patches;
 //  * forage_update_kernel (one warp per agent, one agent per block): private information,
 //    decision processes, mode, random walk / relocation / exploitation stop, move, walls.
-// Decision and motion arithmetic is FP64 (the reference's Python floats); positions,
-// orientation and speed are stored as float32, rounded where the step writes them.  Random
+// Decision and motion arithmetic is FP64 (the reference's Python floats; cos / sin of the new
+// heading in double-float, within 1e-13 of FP64); positions, orientation and speed are stored
+// as float32, rounded where the step writes them.  Random
 // numbers come from a Philox-4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
 // "Parallel random numbers: as easy as 1, 2, 3", SC 2011) keyed by the seed, with one counter
 // per agent and per patch slot, so a step is reproducible and graph-replayable.
@@ -81,6 +82,7 @@ struct ForageArgs {
     int *exploit;      // scratch: 1 where the overriding mode is "exploit"
     const double *uniforms;
     unsigned long long *diag;
+    const float4 *sctab;   // double-float cos/sin table (global copy)
 };
 
 // Agent.get_mode (agent.py:627-639): the overriding mode, else relocate / explore by w.
@@ -448,6 +450,28 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
     const int i = blockIdx.x * kUpdateWarps + (threadIdx.x >> 5);
     if (i >= a.n) return;   // warp-uniform
     const abm_forage_params &p = a.p;
+    // lane 0's state loads are issued first, so their latency overlaps the pixel count
+    uint32_t nov = 0;
+    double col = 0, colb = 0, w = 0, u = 0, r01u = 0;
+    int ovr = 0, mode = 0, env = 0;
+    float v0f = 0, th0f = 0, x0f = 0, y0f = 0;
+    uint64_t draws = 0;
+    if (lane == 0) {
+        nov = a.ag.novelty[i];
+        col = a.ag.collected[i];
+        colb = a.ag.collected_before[i];
+        w = a.ag.w[i];
+        u = a.ag.u[i];
+        ovr = a.ag.override_mode[i];
+        mode = a.ag.mode[i];
+        env = a.ag.env_status[i];
+        v0f = a.ag.v[i];
+        th0f = a.ag.theta[i];
+        x0f = a.ag.x[i];
+        y0f = a.ag.y[i];
+        if (a.uniforms) r01u = a.uniforms[i];
+        else draws = a.ag.draws[i];
+    }
     // social field statistics: mean, and the left / right halves of F_reloc_LR
     const uint32_t *bits = a.soc + (size_t)i * a.words;
     const int rv = p.rv, half = rv / 2;
@@ -463,11 +487,9 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
     left = __reduce_add_sync(ABM_FULL_MASK, left);
     if (lane != 0) return;
     // calc_I_priv (agent.py:180-187): novelty memory and the units collected this step
-    const double I_priv = p.F_N * (a.ag.novelty[i] ? 1.0 : 0.0) +
-                          p.F_R * (a.ag.collected[i] - a.ag.collected_before[i]);
+    const double I_priv = p.F_N * (nov ? 1.0 : 0.0) + p.F_R * (col - colb);
     if (a.ag.ipriv) a.ag.ipriv[i] = I_priv;
     // update_decision_processes (agent.py:194-210)
-    double w = a.ag.w[i], u = a.ag.u[i];
     const double w_p = w > p.T_w ? w : 0.0;
     const double u_p = u > p.T_u ? u : 0.0;
     const double dw = p.Eps_w * ((double)total / rv) - p.g_w * (w - p.B_w) - u_p * p.S_uw;
@@ -481,13 +503,12 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
     a.ag.w[i] = w;
     a.ag.u[i] = u;
     // mode and motion increments (agent.py:223-259); tr_u compares u with T_w (agent.py:622)
-    int ovr = a.ag.override_mode[i], mode = a.ag.mode[i];
-    const double vel0 = (double)a.ag.v[i];
+    const double vel0 = (double)v0f;
     double vel = 0.0, theta = 0.0;
     const int cur = ovr != ABM_MODE_NONE ? ovr : (w > p.T_w ? ABM_MODE_RELOCATE : ABM_MODE_EXPLORE);
     if (cur != ABM_MODE_COLLIDE) {
         const bool tw = w > p.T_w, tu = u > p.T_w;
-        const bool on_patch = a.ag.env_status[i] == 1;
+        const bool on_patch = env == 1;
         int action;   // 0 random walk, 1 relocate, 2 exploit
         if (!tw && !tu) action = 0;
         else if (tw && tu) action = on_patch ? 2 : 1;
@@ -496,12 +517,12 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
         if (action == 0) {   // supcalc.random_walk(desired_vel=max_exp_vel)
             double r01;
             if (a.uniforms) {
-                r01 = a.uniforms[i];
+                r01 = r01u;
             } else {
                 uint32_t wd[4];
-                philox_draw(p.seed, (uint32_t)i, a.ag.draws[i], kTagWalk, wd);
+                philox_draw(p.seed, (uint32_t)i, draws, kTagWalk, wd);
                 r01 = u01(wd[0], wd[1]);
-                a.ag.draws[i] += 1;
+                a.ag.draws[i] = draws + 1;
             }
             vel = p.exp_vel_max;
             theta = p.exp_theta_min + (p.exp_theta_max - p.exp_theta_min) * r01;
@@ -523,14 +544,17 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
     a.ag.mode[i] = mode;
     a.ag.override_mode[i] = ovr;
     // the move (agent.py:263-277), prove_velocity (agent.py:612-620), reflect_from_walls
-    double th = prove_orientation((double)a.ag.theta[i] + theta);
+    double th = prove_orientation((double)th0f + theta);
     double v = vel0 + vel;
     const int after = ovr != ABM_MODE_NONE ? ovr : (w > p.T_w ? ABM_MODE_RELOCATE : ABM_MODE_EXPLORE);
     if (after == ABM_MODE_EXPLORE && fabs(v) > 1.0) v = p.exp_vel_max;
-    double sn, cs;
-    sincos(th, &sn, &cs);
-    double x = (double)a.ag.x[i] + v * cs;
-    double y = (double)a.ag.y[i] - v * sn;
+    // cos / sin of the new heading in double-float on the FP32 pipe (within 1e-13 of FP64; the
+    // position is stored as float32)
+    dfl cd, sd;
+    df_sincos_df(df_split(th), a.sctab, cd, sd);
+    const double cs = (double)cd.hi + (double)cd.lo, sn = (double)sd.hi + (double)sd.lo;
+    double x = (double)x0f + v * cs;
+    double y = (double)y0f - v * sn;
     const double R = p.agent_radius, bx0 = p.window_pad, bx1 = p.window_pad + p.width;
     const double by0 = p.window_pad, by1 = p.window_pad + p.height;
     const double cx = x + R, cy = y + R;
@@ -562,7 +586,7 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
     a.ag.y[i] = (float)y;
     a.ag.theta[i] = (float)th;
     a.ag.v[i] = (float)v;
-    a.ag.collected_before[i] = a.ag.collected[i];
+    a.ag.collected_before[i] = col;
     if (a.diag && !(isfinite(x) && isfinite(y) && isfinite(th) && isfinite(v) && isfinite(w) &&
                     isfinite(u)))
         atomicAdd(&a.diag[ABM_DIAG_NONFINITE], 1ull);
@@ -1293,6 +1317,8 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
     a.exploit = scratch_dev + n;
     a.uniforms = uniforms_dev;
     a.diag = diag_dev;
+    a.sctab = sincos_table_dev(&st);
+    if (!a.sctab) return st;
     if (p->collide_agents) {
         if ((st = allow_dynamic_smem((const void *)forage_collide_kernel, 200 * 1024,
                                      "forage_collide_kernel smem")))
