@@ -13,8 +13,8 @@
 //  * forage_update_kernel (one warp per agent, one agent per block): private information,
 //    decision processes, mode, random walk / relocation / exploitation stop, move, walls.
 // Decision and motion arithmetic is FP64 (the reference's Python floats; cos / sin of the new
-// heading in double-float, within 1e-13 of FP64); positions, orientation and speed are stored
-// as float32, rounded where the step writes them.  Random
+// heading and the turn towards a patch centre in double-float, within 1e-13 of FP64);
+// positions, orientation and speed are stored as float32, rounded where the step writes them.  Random
 // numbers come from a Philox-4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
 // "Parallel random numbers: as easy as 1, 2, 3", SC 2011) keyed by the seed, with one counter
 // per agent and per patch slot, so a step is reproducible and graph-replayable.
@@ -104,6 +104,21 @@ __device__ inline void notify(const ForageArgs &a, int i, int status, int res_id
     a.ag.patch_id[i] = res_id;
 }
 
+// atan2(dy, dx) in double-float on the FP32 pipe: the FP32 angle a0, refined by the angle of
+// the offset rotated by -a0 (below 1e-6 rad, so its tangent w / u gives it to ~1e-18).  Within
+// ~1e-13 rad of the exact angle; atan2(0, 0) = 0 as in FP64.
+__device__ dfl df_atan2(double dy, double dx, const float4 *tab) {
+    const float a0 = atan2f((float)dy, (float)dx);
+    dfl c0, s0;
+    df_sincos_df(dfl{a0, 0.f}, tab, c0, s0);
+    const dfl X = df_split(dx), Y = df_split(dy);
+    const dfl u = df_add(df_mul(X, c0), df_mul(Y, s0));
+    const dfl w = df_sub(df_mul(Y, c0), df_mul(X, s0));
+    const float uf = u.hi + u.lo;
+    const float delta = uf != 0.f ? (w.hi + w.lo) / uf : 0.f;
+    return two_sum(a0, delta);
+}
+
 // The sims.py:821-823 notification condition.
 __device__ inline bool pooling_done(const ForageArgs &a, int i, int m) {
     return ((m == ABM_MODE_POOL || m == ABM_MODE_RELOCATE) && a.ag.pool_success[i]) ||
@@ -160,11 +175,18 @@ __device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed, int *mq)
     //     free: they are independent given D) and run 32 at a time, so the FP64 turn below is
     //     issued once per 32 members rather than once per 32 agents.
     auto member = [&](int i) {
-        // bias_agent_towards_res_center (sims.py:544-552)
+        // bias_agent_towards_res_center (sims.py:544-552): orientation += ((atan2 + orientation)
+        // % 2 pi - pi) * 0.02, in double-float (within ~1e-14 of FP64 before the float32 store)
         const double dx = pcx - ((double)a.ag.x[i] + R), dy = pcy - ((double)a.ag.y[i] + R);
-        double cl = fmod(atan2(dy, dx) + (double)a.ag.theta[i], 2.0 * M_PI);
-        if (cl < 0) cl += 2.0 * M_PI;   // Python's % with a positive divisor
-        a.ag.theta[i] = (float)((double)a.ag.theta[i] + (cl - M_PI) * 0.02);
+        const float thf = a.ag.theta[i];
+        const dfl two_pi = df_split(2.0 * M_PI), pi = df_split(M_PI);
+        dfl cl = df_add(df_atan2(dy, dx, a.sctab), dfl{thf, 0.f});
+        // Python's % with a positive divisor (collision turns may have left the orientation a
+        // little outside [0, 2 pi]: a few wraps at most)
+        for (int k2 = 0; k2 < 4 && df_sign(cl) < 0; ++k2) cl = df_add(cl, two_pi);
+        for (int k2 = 0; k2 < 4 && df_sign(df_sub(cl, two_pi)) >= 0; ++k2) cl = df_sub(cl, two_pi);
+        const dfl tn = df_add(dfl{thf, 0.f}, df_mul(df_sub(cl, pi), df_split(0.02)));
+        a.ag.theta[i] = (float)((double)tn.hi + (double)tn.lo);
         if (i > D) {
             notify(a, i, -1, -1);
             notify(a, i, -1, -1);
