@@ -12,7 +12,7 @@ The oracle is an FP64 C restatement (``vpf_oracle.c``) of the reference function
 * ``supcalc.find_nearest`` / ``angle_between``  abm/agent/supcalc.py:8-34
 
 wrapped here with ctypes.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
-leg of ``bench.py`` use it, always as the checker or the timed CPU baseline; the library never
+leg of ``bench.py`` use it, always as the reference results or the timed CPU baseline; the library never
 imports it.  It is pinned against fixtures produced by the reference itself
 (``tests/golden/make_golden.py``) and the reference's own known-answer vectors.
 """

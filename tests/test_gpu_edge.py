@@ -2,7 +2,7 @@
 torch.autograd.Function in abm_gb300.edge):
 
 * forward integrals against the FP64 reference (tests/_edge_ref.py);
-* the pixel VPF at high Rv converges to the edge form (the pixel path is the judge);
+* the pixel VPF at high Rv converges to the edge form (the pixel path is the arbiter);
 * adjoint gradients (alp0, alp1, beta0, beta1, v0 and the initial state) against FP64 autograd
   and against FP64 central finite differences (h = 1e-4): within 1e-4 relative.
 """
