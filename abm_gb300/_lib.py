@@ -141,6 +141,14 @@ SIGNATURES = [
      [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32, c_i32_p, c_i32_p,
       c_i32_p, ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_u32_p,
       c_double_p, c_u64_p, c_void_p]),
+    ("abm_vpf_flock_run", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
+      ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_int32, c_int32, c_u64_p,
+      c_void_p]),
+    ("abm_vpf_flock_batched_run", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32, c_i32_p, c_i32_p,
+      c_i32_p, ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_int32, c_int32,
+      c_u64_p, c_void_p]),
     ("abm_vpf_flock_step_noalloc", c_int32,
      [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
       ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_u32_p, c_double_p,

@@ -1041,6 +1041,52 @@ __global__ void __launch_bounds__(32 * kVswrmWarps) vswrm_kernel(const VswrmArgs
 
 using namespace abm;
 
+// ---------------------------------------------------------------------------- multi-step runs
+// `steps` steps of one(in, out) between the states a and b: one eager step a -> b (it builds
+// the grid tables and the stream's workspace, which no graph capture may do), then whole
+// chunks of `chunk` (even) steps replayed from a graph captured on the stream, then the rest
+// eagerly.  The final state is in a after an even number of steps, in b after an odd one.
+// A legacy default stream (NULL) cannot be captured: every step is then launched eagerly.
+template <class StepFn>
+static int run_steps(abm_swarm_state *a, abm_swarm_state *b, int steps, int chunk,
+                     cudaStream_t s, StepFn one, const char *fn) {
+    if (steps < 0 || chunk < 0)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: steps=%d graph_chunk=%d", fn, steps, chunk);
+    if (steps == 0) return ABM_OK;
+    int warn = one(a, b);
+    if (warn < 0) return warn;
+    int done = 1;
+    chunk &= ~1;
+    if (s != nullptr && chunk >= 2 && steps - done >= chunk) {
+        int st = check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                            "cudaStreamBeginCapture");
+        if (st) return st;
+        int step_st = ABM_OK;
+        for (int k = 0; k < chunk && step_st >= 0; ++k) step_st = (k % 2 == 0) ? one(b, a) : one(a, b);
+        cudaGraph_t graph = nullptr;
+        st = check_cuda(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
+        if (step_st < 0 || st) {
+            if (graph) cudaGraphDestroy(graph);
+            return step_st < 0 ? step_st : st;
+        }
+        cudaGraphExec_t exec = nullptr;
+        st = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+        cudaGraphDestroy(graph);
+        if (st) return st;
+        while (steps - done >= chunk && !st) {   // b -> ... -> b
+            st = check_cuda(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+            done += chunk;
+        }
+        cudaGraphExecDestroy(exec);   // freed once its launches complete
+        if (st) return st;
+    }
+    for (; done < steps; ++done) {
+        const int st = (done % 2 == 1) ? one(b, a) : one(a, b);
+        if (st < 0) return st;
+    }
+    return warn;
+}
+
 extern "C" {
 
 int abm_vpf_set_step_config(int32_t warps_per_block, int32_t tile) {
@@ -1297,6 +1343,31 @@ int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32
     return step_launch(in, out, n_total, p, ov, vpf_bits_dev, terms_dev, diag_dev,
                        (cudaStream_t)stream, g, sctab, ws, fn, seg_begin_dev,
                        seg_end_dev, order_dev);
+}
+
+int abm_vpf_flock_run(abm_swarm_state *a, abm_swarm_state *b, int32_t n,
+                      const abm_vf_params *p, const abm_agent_overrides *ov, int32_t steps,
+                      int32_t graph_chunk, unsigned long long *diag_dev, void *stream) {
+    const char *fn = "abm_vpf_flock_run";
+    if (!a || !b) return set_error(ABM_ERR_INVALID_ARG, "%s: NULL state", fn);
+    auto one = [&](abm_swarm_state *in, abm_swarm_state *out) {
+        return abm_vpf_flock_step(in, out, n, p, ov, nullptr, nullptr, diag_dev, stream);
+    };
+    return run_steps(a, b, steps, graph_chunk, (cudaStream_t)stream, one, fn);
+}
+
+int abm_vpf_flock_batched_run(abm_swarm_state *a, abm_swarm_state *b, int32_t n_total,
+                              const int32_t *seg_begin_dev, const int32_t *seg_end_dev,
+                              const int32_t *order_dev, const abm_vf_params *p,
+                              const abm_agent_overrides *ov, int32_t steps, int32_t graph_chunk,
+                              unsigned long long *diag_dev, void *stream) {
+    const char *fn = "abm_vpf_flock_batched_run";
+    if (!a || !b) return set_error(ABM_ERR_INVALID_ARG, "%s: NULL state", fn);
+    auto one = [&](abm_swarm_state *in, abm_swarm_state *out) {
+        return abm_vpf_flock_batched(in, out, n_total, seg_begin_dev, seg_end_dev, order_dev, p,
+                                     ov, nullptr, nullptr, diag_dev, stream);
+    };
+    return run_steps(a, b, steps, graph_chunk, (cudaStream_t)stream, one, fn);
 }
 
 int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, int32_t n,

@@ -93,11 +93,24 @@ class VFSwarm:
         steps = int(self._pol_step.item())
         return self._pol[0, : min(steps, self._pol.shape[1])].cpu().numpy()
 
-    def run(self, steps: int, stream=None) -> int:
-        st = 0
-        for _ in range(steps):
-            st = self.step(stream=stream)
-        return st
+    def run(self, steps: int, stream=None, graph_chunk: int = 0) -> int:
+        """Advance `steps` steps.  graph_chunk >= 2: one library call (abm_vpf_flock_run) that
+        replays a CUDA graph of graph_chunk steps (not with polarisation tracking); the stream
+        must then be a non-default one.  Otherwise one abm_vpf_flock_step call per step."""
+        if graph_chunk < 2 or getattr(self, "_pol", None) is not None:
+            st = 0
+            for _ in range(steps):
+                st = self.step(stream=stream)
+            return st
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        status = self.lib.abm_vpf_flock_run(
+            ctypes.byref(self._state_struct(self._cur)), ctypes.byref(self._state_struct(self._nxt)),
+            self.n, ctypes.byref(self._cparams), ctypes.byref(self._ov), int(steps),
+            int(graph_chunk), _lib.u64ptr(self.diag), ctypes.c_void_p(s.cuda_stream))
+        self.last_status = _lib.check(status, "abm_vpf_flock_run")
+        if steps % 2:
+            self._cur, self._nxt = self._nxt, self._cur
+        return self.last_status
 
     # ------------------------------------------------------------------ state access
     @property

@@ -177,6 +177,27 @@ int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32
                           double *terms_dev, unsigned long long *diag_dev, void *stream);
 
 /*
+ * Many steps in one call (the reference's simulation loop over VFSimulation.step_sim,
+ * vf_sims.py:291-340, for `steps` timesteps; for a sweep, its per-configuration runs of
+ * metarunner.py:240-254 for all configurations at once): the state ping-pongs between a and b,
+ * starting from a; after an even number of steps the result is in a, after an odd number in b.
+ * The library runs one step eagerly, then replays a CUDA graph of graph_chunk steps (rounded
+ * down to an even number; 0 or 1: no graph) captured on `stream`, then the remaining steps
+ * eagerly.  Results are those of the same number of abm_vpf_flock_step / _batched calls.  A
+ * NULL (legacy default) stream cannot be captured: every step is then launched eagerly.  Call
+ * it outside any stream capture of the caller's own.  Status: the first step's (0 or
+ * ABM_WARN_PHI_MISMATCH) or an error.
+ */
+int abm_vpf_flock_run(abm_swarm_state *a, abm_swarm_state *b, int32_t n, const abm_vf_params *p,
+                      const abm_agent_overrides *ov, int32_t steps, int32_t graph_chunk,
+                      unsigned long long *diag_dev, void *stream);
+int abm_vpf_flock_batched_run(abm_swarm_state *a, abm_swarm_state *b, int32_t n_total,
+                              const int32_t *seg_begin_dev, const int32_t *seg_end_dev,
+                              const int32_t *order_dev, const abm_vf_params *p,
+                              const abm_agent_overrides *ov, int32_t steps, int32_t graph_chunk,
+                              unsigned long long *diag_dev, void *stream);
+
+/*
  * abm_vpf_flock_step on HOST state (no counterpart in the reference; the call a host-side
  * loop makes once per step): in_host / out_host hold host pointers (x, y, theta, v).  For
  * memory registered with CUDA (page-locked, e.g. cudaHostAlloc or torch pin_memory, or
