@@ -188,6 +188,10 @@ SIGNATURES = [
      [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
       ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), ctypes.c_void_p]),
     ("abm_forage_params_default", c_int32, [ctypes.POINTER(AbmForageParams)]),
+    ("abm_forage_run", c_int32,
+     [ctypes.POINTER(AbmForagerState), c_int32, ctypes.POINTER(AbmPatchState), c_int32,
+      ctypes.POINTER(AbmForageParams), c_u32_p, c_i32_p, c_int32, c_int32,
+      ctypes.POINTER(AbmForageRecording), c_u64_p, ctypes.c_void_p]),
     ("abm_forage_step", c_int32,
      [ctypes.POINTER(AbmForagerState), c_int32, ctypes.POINTER(AbmPatchState), c_int32,
       ctypes.POINTER(AbmForageParams), c_u32_p, c_i32_p, c_double_p, c_u64_p, ctypes.c_void_p]),

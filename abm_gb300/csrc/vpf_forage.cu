@@ -1366,4 +1366,55 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
     return check_cuda(cudaGetLastError(), "forage_update_kernel launch");
 }
 
+int abm_forage_run(abm_forager_state *agents, int32_t n, abm_patch_state *patches,
+                   int32_t n_patches, const abm_forage_params *p, uint32_t *soc_bits_dev,
+                   int32_t *scratch_dev, int32_t steps, int32_t graph_chunk,
+                   abm_forage_recording *rec, unsigned long long *diag_dev, void *stream) {
+    const char *fn = "abm_forage_run";
+    if (steps < 0 || graph_chunk < 0)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: steps=%d graph_chunk=%d", fn, steps,
+                         graph_chunk);
+    cudaStream_t s = (cudaStream_t)stream;
+    auto one = [&]() {
+        int st = abm_forage_step(agents, n, patches, n_patches, p, soc_bits_dev, scratch_dev,
+                                 nullptr, diag_dev, stream);
+        if (st >= 0 && rec)
+            st = abm_forage_record(agents, n, patches, n_patches, soc_bits_dev, p->rv, rec,
+                                   stream);
+        return st;
+    };
+    if (steps == 0) return ABM_OK;
+    int st = one();   // eager: tables and kernel attributes are set up outside any capture
+    if (st < 0) return st;
+    int done = 1;
+    if (s != nullptr && graph_chunk >= 1 && steps - done >= graph_chunk) {
+        st = check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                        "cudaStreamBeginCapture");
+        if (st) return st;
+        int step_st = ABM_OK;
+        for (int k = 0; k < graph_chunk && step_st >= 0; ++k) step_st = one();
+        cudaGraph_t graph = nullptr;
+        st = check_cuda(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
+        if (step_st < 0 || st) {
+            if (graph) cudaGraphDestroy(graph);
+            return step_st < 0 ? step_st : st;
+        }
+        cudaGraphExec_t exec = nullptr;
+        st = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+        cudaGraphDestroy(graph);
+        if (st) return st;
+        while (steps - done >= graph_chunk && !st) {
+            st = check_cuda(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+            done += graph_chunk;
+        }
+        cudaGraphExecDestroy(exec);   // freed once its launches complete
+        if (st) return st;
+    }
+    for (; done < steps; ++done) {
+        st = one();
+        if (st < 0) return st;
+    }
+    return ABM_OK;
+}
+
 }  // extern "C"

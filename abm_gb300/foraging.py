@@ -365,6 +365,24 @@ class ForagingSim:
         for _ in range(steps):
             self.step()
 
+    def run_in_library(self, steps: int, graph_chunk: int = 100, stream=None) -> int:
+        """Advance `steps` steps with one abm_forage_run call (the library captures and replays
+        its own CUDA graph of graph_chunk steps on `stream`, a non-default one; recording, when
+        enabled, after every step).  Same state as `steps` calls of step()."""
+        s = stream if stream is not None else torch.cuda.Stream(self.device)
+        if stream is None:
+            s.wait_stream(torch.cuda.current_stream(self.device))
+        st = _lib.check(self.lib.abm_forage_run(
+            ctypes.byref(self._agent_struct), self.n, ctypes.byref(self._patch_struct), self.np,
+            ctypes.byref(self._cparams), _lib.u32ptr(self.soc_bits), _lib.i32ptr(self.scratch),
+            int(steps), int(graph_chunk),
+            ctypes.byref(self._rec_struct) if self.rec is not None else None,
+            _lib.u64ptr(self.diag), ctypes.c_void_p(s.cuda_stream)), "abm_forage_run")
+        if stream is None:
+            torch.cuda.current_stream(self.device).wait_stream(s)
+        self.t += int(steps)
+        return st
+
     def agents_numpy(self) -> dict:
         out = {}
         for k, dt in AGENT_FIELDS:

@@ -146,6 +146,20 @@ int abm_forage_record(const abm_forager_state *agents, int32_t n, const abm_patc
                       int32_t n_patches, const uint32_t *soc_bits_dev, int32_t rv,
                       abm_forage_recording *rec, void *stream);
 
+/*
+ * `steps` foraging steps in one call (the reference's Simulation.start loop for T steps), each
+ * followed by abm_forage_record when rec is non-NULL: one step eagerly, then a CUDA graph of
+ * graph_chunk steps (0: no graph) captured on `stream` and replayed, then the remaining steps
+ * eagerly.  The random walk uses the agents' Philox streams (no injected uniforms).  Same
+ * results as the same number of abm_forage_step (+ abm_forage_record) calls.  A NULL (legacy
+ * default) stream cannot be captured: every step is then launched eagerly.  Call it outside
+ * any stream capture of the caller's own.
+ */
+int abm_forage_run(abm_forager_state *agents, int32_t n, abm_patch_state *patches,
+                   int32_t n_patches, const abm_forage_params *p, uint32_t *soc_bits_dev,
+                   int32_t *scratch_dev, int32_t steps, int32_t graph_chunk,
+                   abm_forage_recording *rec, unsigned long long *diag_dev, void *stream);
+
 /* Philox-4x32-10 block for (counter, key): the generator of abm_forage_step, exported for
  * the tests (host function, no GPU needed). */
 void abm_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

@@ -81,3 +81,28 @@ def test_run_rejects_bad_arguments():
     st = s.lib.abm_vpf_flock_run(None, None, s.n, ctypes.byref(s._cparams), None, 4, 2, None,
                                  None)
     assert st == _lib.ABM_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("collide,steps,chunk", [(False, 250, 100), (True, 130, 40),
+                                                 (False, 7, 100)])
+def test_forage_run_matches_single_steps(collide, steps, chunk):
+    """abm_forage_run (library graph of graph_chunk steps) = single abm_forage_step calls,
+    recording included."""
+    from abm_gb300.foraging import ForageParams, ForagingSim
+    prm = ForageParams(seed=12, min_resc_units=20, max_resc_units=60, collide_agents=collide,
+                       width=400.0, height=400.0, rv=400)
+    a = ForagingSim(prm, n_agents=60, n_patches=3, init_seed=4, record_steps=steps)
+    b = ForagingSim(prm, n_agents=60, n_patches=3, init_seed=4, record_steps=steps)
+    for _ in range(steps):
+        a.step()
+    b.run_in_library(steps, graph_chunk=chunk)
+    torch.cuda.synchronize()
+    sa, sb = a.agents_numpy(), b.agents_numpy()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+    pa, pb = a.patches_numpy(), b.patches_numpy()
+    for k in pa:
+        assert np.array_equal(pa[k], pb[k]), k
+    ra, rb = a.recording(), b.recording()
+    for k in ra:
+        assert np.array_equal(np.asarray(ra[k]), np.asarray(rb[k])), k
