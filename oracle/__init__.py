@@ -78,6 +78,8 @@ def lib():
             L.orc_closed_angle_agent.restype = c_d
             L.orc_projection_field.argtypes = [c_d, c_d, c_int, c_d, c_d, c_d, c_d, c_int, dp, dp,
                                                c_int, c_d, c_d, c_d, dp, dp]
+            L.orc_projection_union.argtypes = [c_d, c_d, c_int, c_d, c_d, c_d, c_d, c_int, dp,
+                                               dp, c_int, c_d, c_d, dp, dp]
             L.orc_dphi_v.argtypes = [dp, c_int, dp]
             L.orc_vswrm.argtypes = [c_d, dp, dp, c_int, dp, c_d, c_d, c_d, dp]
             L.orc_vf_step.argtypes = [c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp, c_int, dp, dp,
@@ -158,6 +160,23 @@ def projection_field(fov, v_field_resolution, position, radius, orientation, obj
                                float("nan") if vision_range is None else float(vision_range),
                                _dp(out), _dp(marg))
     return (out, marg) if return_margins else out
+
+
+def projection_union(fov, v_field_resolution, position, radius, orientation, object_positions,
+                     object_sizes=None, infinite=False, arena_width=0.0, arena_height=0.0):
+    """The OR of projection_field's rows in raw pixel order (calc_soc_v_proj's binarised sum,
+    unflipped) without materialising the rows, and each object's decision margin."""
+    objs = _f64(np.asarray(object_positions, dtype=np.float64).reshape(-1, 2))
+    n = objs.shape[0]
+    sizes = None if object_sizes is None else _f64(np.asarray(object_sizes, np.float64))
+    V = np.zeros(v_field_resolution, np.float64)
+    marg = np.zeros(n, np.float64)
+    lib().orc_projection_union(float(fov[0]), float(fov[1]), int(v_field_resolution),
+                               float(position[0]), float(position[1]), float(radius),
+                               float(orientation), n, _dp(objs), _dp(sizes),
+                               1 if infinite else 0, float(arena_width), float(arena_height),
+                               _dp(V), _dp(marg))
+    return V, marg
 
 
 def dphi_v(V) -> np.ndarray:

@@ -138,6 +138,35 @@ def test_full_size_spot_check_cfg2():
         _check_terms(terms[i], ref, i)
 
 
+def test_max_size_spot_check_tiled():
+    """The largest sizes: N=17000 agents (above 16384, so the automatic choice is the tiled
+    form with TMA-staged, double-buffered neighbour tiles) and Rv=16384 (the maximum), R=3 in
+    12000x12000; 4 focal agents recomputed by the oracle (union of the rows, no dense
+    materialisation)."""
+    n, rv, R, W = 17000, 16384, 3.0, 12000.0
+    p = dict(gam=0.1, v0=1.0, alp0=1.0, alp1=0.08, alp2=0.0, bet0=1.0, bet1=0.08, bet2=0.0,
+             boundary=0, limit_movement=0, max_vel=3.0, max_th=0.1, width=W, height=W,
+             window_pad=30.0, fov0=-np.pi, fov1=np.pi, rv=rv, radius=R, dt=1.0)
+    st = seeded_swarm(77, n, W, W, R=R, kappa=None)
+    sw = _swarm_from(st, p)
+    sw.step(want_vpf=True, want_terms=True)
+    terms = sw.terms.cpu().numpy()
+    d = sw.diagnostics()
+    assert d["timeouts"] == 0 and d["nonfinite"] == 0
+    rng = np.random.default_rng(1)
+    phi = oracle.arange_phi(rv)
+    for i in rng.choice(n, 4, replace=False):
+        words = sw.vpf_bits[i].cpu().numpy().view(np.uint32)
+        gpu = np.unpackbits(words.view(np.uint8), bitorder="little")[:rv]
+        objs = np.stack([np.delete(st["x"], i), np.delete(st["y"], i)], axis=1)
+        V, marg = oracle.projection_union((-np.pi, np.pi), rv, [st["x"][i], st["y"][i]], R,
+                                          st["theta"][i], objs)
+        bad = np.where(gpu != V.astype(np.uint8))[0]
+        assert len(bad) == 0 or np.min(marg) < 1e-9, (i, bad[:10])
+        ref = oracle.vswrm(st["v"][i], phi, V, p)
+        _check_terms(terms[i], ref, i)
+
+
 def test_permutation_invariance_full_size():
     """The VPF is a union of intervals: reordering the agents must permute the outputs
     exactly (N=4096, Rv=3600)."""
