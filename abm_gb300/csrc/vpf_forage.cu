@@ -83,6 +83,9 @@ struct ForageArgs {
     const double *uniforms;
     unsigned long long *diag;
     const float4 *sctab;   // double-float cos/sin table (global copy)
+    // 1 / Rv, 1 / (Rv / 2), 1 / (Rv - Rv / 2) for the social field's means (within one FP64
+    // ulp of the divisions), and the linspace pixel step 2 pi / (Rv - 1) (the FP64 division)
+    double inv_rv, inv_half, inv_rest, px_step, inv_px_step;
 };
 
 // Agent.get_mode (agent.py:627-639): the overriding mode, else relocate / explore by w.
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
     // update_decision_processes (agent.py:194-210)
     const double w_p = w > p.T_w ? w : 0.0;
     const double u_p = u > p.T_u ? u : 0.0;
-    const double dw = p.Eps_w * ((double)total / rv) - p.g_w * (w - p.B_w) - u_p * p.S_uw;
+    const double dw = p.Eps_w * ((double)total * a.inv_rv) - p.g_w * (w - p.B_w) - u_p * p.S_uw;
     const double du = p.Eps_u * I_priv - p.g_u * (u - p.B_u) - w_p * p.S_wu;
     w += dw;
     u += du;
@@ -551,7 +554,8 @@ __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(Forage
             mode = ABM_MODE_EXPLORE;
             ovr = ABM_MODE_NONE;
         } else if (action == 1) {   // supcalc.F_reloc_LR(v, soc_v_field, max_exp_vel)
-            const double le = (double)left / half, re = (double)(total - left) / (rv - half);
+            const double le = (double)left * a.inv_half;
+            const double re = (double)(total - left) * a.inv_rest;
             vel = p.exp_vel_max - vel0;
             theta = (le - re) * p.reloc_theta_max;
             mode = ABM_MODE_RELOCATE;
@@ -916,8 +920,8 @@ __global__ void __launch_bounds__(kCollideBlock) forage_collide_kernel(ForageArg
             rank[r] = e;
         }
         __syncthreads();
-        const double step = __ddiv_rn(__dsub_rn(kPi, -kPi), (double)(rv - 1));
-        const float inv_stepf = (float)(1.0 / step), stepf = (float)step;
+        const double step = a.px_step;
+        const float inv_stepf = (float)a.inv_px_step, stepf = (float)step;
         int *writer = reinterpret_cast<int *>(val + kCollideMaxNodes);   // after the node values
         // FP32 bearing guard: the FP32 angle is within 1.5e-6 rad of the exact one (heading
         // rounded to float, sincosf, products, atan2f); decisions closer than this to a pixel
@@ -973,7 +977,7 @@ __global__ void __launch_bounds__(kCollideBlock) forage_collide_kernel(ForageArg
                     const double ca = closed_angle_unit_f64(u1x, u1y, E.u2x, E.u2y);
                     if (!(-kPi < ca && ca < kPi)) continue;   // outside the full-circle FOV
                     // supcalc.find_nearest on np.linspace(-pi, pi, rv): argmin, first on ties
-                    const double kf = floor((ca + kPi) * (1.0 / step) + 0.5);
+                    const double kf = floor((ca + kPi) * a.inv_px_step + 0.5);
                     const int k0 = (int)fmin(fmax(kf, 0.0), (double)(rv - 1));
                     double best = INFINITY;
                     int t = 0;
@@ -1341,6 +1345,11 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
     a.diag = diag_dev;
     a.sctab = sincos_table_dev(&st);
     if (!a.sctab) return st;
+    a.inv_rv = 1.0 / p->rv;
+    a.inv_half = 1.0 / (p->rv / 2);
+    a.inv_rest = 1.0 / (p->rv - p->rv / 2);
+    a.px_step = (kPi - (-kPi)) / (double)(p->rv - 1);   // np.linspace(-pi, pi, Rv) step
+    a.inv_px_step = 1.0 / a.px_step;                     // estimates only
     if (p->collide_agents) {
         if ((st = allow_dynamic_smem((const void *)forage_collide_kernel, 200 * 1024,
                                      "forage_collide_kernel smem")))
