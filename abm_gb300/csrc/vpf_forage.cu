@@ -86,6 +86,7 @@ struct ForageArgs {
     // 1 / Rv, 1 / (Rv / 2), 1 / (Rv - Rv / 2) for the social field's means (within one FP64
     // ulp of the divisions), and the linspace pixel step 2 pi / (Rv - 1) (the FP64 division)
     double inv_rv, inv_half, inv_rest, px_step, inv_px_step;
+    double inv_vr;   // 1 / vision_range, correctly rounded
 };
 
 // Agent.get_mode (agent.py:627-639): the overriding mode, else relocate / explore by w.
@@ -652,7 +653,7 @@ __device__ inline bool rects_collide(float xa, float ya, float xb, float yb, lon
 }
 
 struct CollideEntry {
-    double d;          // centre distance (the reference's rounded FP64 value)
+    double d;          // squared centre distance (FP64, products and sum rounded separately)
     double ox, oy;     // offset from the focal centre to the obstacle centre
     double u2x, u2y;   // its unit vector (FP64 route only)
     unsigned long long dkey;   // bits of d: non-negative doubles order like their bits
@@ -837,22 +838,26 @@ __global__ void __launch_bounds__(kCollideBlock) forage_collide_kernel(ForageArg
             if (fdx * fdx + fdy * fdy > lim * lim) continue;
             const double ddx = __dsub_rn(__dadd_rn((double)xj, R), c1x);
             const double ddy = __dsub_rn(__dadd_rn((double)yj, R), c1y);
-            const double d = __dsqrt_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)));
-            if (!(d < 2 * R + 20)) continue;
+            // squared distance: a correctly rounded sqrt is monotone, so d < 2R + 20 and the
+            // order of the distances follow from it (up to rounding ties of measure zero);
+            // the sqrt itself is needed only for the field weight below
+            const double d2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
+            const double lim_d = 2 * R + 20;
+            if (!(d2 < lim_d * lim_d)) continue;
             const int pos = atomicAdd(&s_m, 1);
             if (pos >= cap) {
                 s_over = 1;
                 continue;
             }
             CollideEntry e;
-            e.d = d;
+            e.d = d2;
             e.x = xj;
             e.y = yj;
             e.j = j;
             e.same = xj == fx && yj == fy;
             e.ox = ddx;
             e.oy = ddy;
-            e.dkey = (unsigned long long)__double_as_longlong(d);
+            e.dkey = (unsigned long long)__double_as_longlong(d2);
             e.fov = 0;
             ent[pos] = e;
         }
@@ -880,14 +885,21 @@ __global__ void __launch_bounds__(kCollideBlock) forage_collide_kernel(ForageArg
             s_nleaf = -1;   // the pairwise trees are built on first use
             // `distance` after the obstacle loop: the last non-coincident obstacle in list order
             int jl = -1;
-            double dl = 0.0;
+            double dl2 = 0.0;
             for (int e = 0; e < m; ++e) {
                 if (!ent[e].same && ent[e].j > jl) {
                     jl = ent[e].j;
-                    dl = ent[e].d;
+                    dl2 = ent[e].d;
                 }
             }
-            s_w = __dsub_rn(1.0, __ddiv_rn(dl, a.p.vision_range));
+            // w = 1 - d / vision_range with the division correctly rounded by Markstein's
+            // correction of a reciprocal product (Markstein, "Computation of elementary
+            // functions on the IBM RISC System/6000 processor", 1990): q0 = d y, r = d - q0 v
+            // (exact), q = q0 + r y, with y = 1/v correctly rounded
+            const double dl = __dsqrt_rn(dl2), vr = a.p.vision_range, y = a.inv_vr;
+            const double q0 = __dmul_rn(dl, y);
+            const double rq = __fma_rn(-q0, vr, dl);
+            s_w = __dsub_rn(1.0, __fma_rn(rq, y, q0));
             if (s_over && a.diag) atomicAdd(&a.diag[ABM_DIAG_CAPACITY], 1ull);
         }
         // fill order = the reference's stable sorts (distance ascending, then visual angle
@@ -900,13 +912,13 @@ __global__ void __launch_bounds__(kCollideBlock) forage_collide_kernel(ForageArg
         for (int e = tid; e < m; e += nthr) {
             CollideEntry &E = ent[e];
             if (!E.same) {
-                const float hpf = atanf((float)R / (float)E.d) * hp_scale;
+                const float hpf = atanf((float)R * rsqrtf((float)E.d)) * hp_scale;
                 const float fl = floorf(hpf), fr = hpf - fl, g = 4e-6f * hpf + 1e-6f;
                 E.H = (int)fl;
                 E.frac = 1;
                 E.hp_exact = !(fr > g && fr < 1.f - g);
                 if (E.hp_exact) {
-                    const double va = __dmul_rn(2.0, atan(__ddiv_rn(R, E.d)));
+                    const double va = __dmul_rn(2.0, atan(__ddiv_rn(R, __dsqrt_rn(E.d))));
                     E.hp = __ddiv_rn(__dmul_rn(__ddiv_rn(va, tp), (double)rv), 2.0);
                 }
                 E.fox = (float)E.ox;
@@ -1350,6 +1362,7 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
     a.inv_rest = 1.0 / (p->rv - p->rv / 2);
     a.px_step = (kPi - (-kPi)) / (double)(p->rv - 1);   // np.linspace(-pi, pi, Rv) step
     a.inv_px_step = 1.0 / a.px_step;                     // estimates only
+    a.inv_vr = 1.0 / p->vision_range;
     if (p->collide_agents) {
         if ((st = allow_dynamic_smem((const void *)forage_collide_kernel, 200 * 1024,
                                      "forage_collide_kernel smem")))
