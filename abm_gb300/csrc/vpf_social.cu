@@ -100,6 +100,20 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
     int *sidx = reinterpret_cast<int *>(smem + L.sidx);     // entries by ascending distance
     int2 *trim = reinterpret_cast<int2 *>(smem + L.trim);   // trimmed (start, end) per entry
     uint4 *srt = reinterpret_cast<uint4 *>(smem + L.srt);   // by rank: key hi, key lo, s0, e0
+    // the first chunk of candidates is loaded now, overlapping the focal agent's set-up (the
+    // loop below loads each next chunk while it classifies the current one)
+    auto load_cand = [&](int j, float &xj, float &yj, float &rj, int &ej, int &pj) {
+        if (j < a.n) {
+            xj = a.x[j];
+            yj = a.y[j];
+            rj = a.radius ? a.radius[j] : a.radius0;
+            ej = a.exploit[j];
+            pj = a.patch[j];
+        }
+    };
+    float cx_ = 0.f, cy_ = 0.f, cr_ = a.radius0;
+    int ce_ = 0, cp_ = 0;
+    load_cand(tid, cx_, cy_, cr_, ce_, cp_);
     for (int w = tid; w < words; w += nthr) vb[w] = 0u;
     if (tid == 0) {
         s_count = 0;
@@ -130,9 +144,10 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
         const int j = jb + tid;
         bool keep = false;
         SocialEntry e;
+        const float xj = cx_, yj = cy_, rj = cr_;
+        const int ej = ce_, pj = cp_;
+        load_cand(j + nthr, cx_, cy_, cr_, ce_, cp_);
         if (j < a.n) {
-            const float xj = a.x[j], yj = a.y[j];
-            const float rj = a.radius ? a.radius[j] : a.radius0;
             // supcalc.distance with each agent's own radius (agent.py:400)
             const dfl dr = two_sum(rj, -ri);
             const dfl ox = df_add(two_sum(xj, -xi), dr), oy = df_add(two_sum(yj, -yi), dr);
@@ -143,10 +158,10 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
             // exploiter of patch -1 on another patch is dropped
             int group = -1;
             if (in_range) {
-                const bool expl = (j != i) && a.exploit[j];
+                const bool expl = (j != i) && ej;
                 if (!expl) group = 1;
-                else if (a.patchwise && a.patch[j] == pi) group = 2;
-                else if (a.patch[j] != -1) group = 0;
+                else if (a.patchwise && pj == pi) group = 2;
+                else if (pj != -1) group = 0;
             }
             if (group > 0 && !a.visual_exclusion) group = -1;  // occluders only with exclusion
             const bool same = (xj == xi) && (yj == yi);         // agent.py:500
@@ -225,6 +240,7 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
         const unsigned kh = float_order_key(ent[e].dkh), kl = float_order_key(ent[e].dkl);
         const int ko = ent[e].ord;
         int rank = 0;
+#pragma unroll 4
         for (int q = 0; q < m; ++q) {
             const unsigned oh = float_order_key(ent[q].dkh), ol = float_order_key(ent[q].dkl);
             const int oo = ent[q].ord;
@@ -241,6 +257,7 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
         const uint4 F = srt[r];
         int sx = (int)F.z, ex = (int)F.w;
         if (a.visual_exclusion) {
+#pragma unroll 4
             for (int q = 0; q < r; ++q) {
                 const uint4 I = srt[q];
                 if (!((I.x < F.x) || (I.x == F.x && I.y < F.y))) continue;   // strictly closer
