@@ -141,10 +141,28 @@ __device__ inline bool pooling_done(const ForageArgs &a, int i, int m) {
 // (without D, members just take their pooling notification and their want).  The turn
 // towards the patch centre reads only the agent's own position and orientation and comes
 // first for every member.
-__device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed, int *mq) {
-    const int lane = threadIdx.x & 31;
+// bias_agent_towards_res_center (sims.py:544-552) for an agent at (x, y) with orientation th
+// on patch k: th + ((atan2 + th) % 2 pi - pi) * 0.02, in double-float (within ~1e-14 of FP64
+// before the float32 store).
+__device__ float turned_orientation(const ForageArgs &a, int k, float x, float y, float thf) {
     const double R = a.p.agent_radius;
     const double pcx = a.pt.x[k] + a.pt.radius[k], pcy = a.pt.y[k] + a.pt.radius[k];
+    const double dx = pcx - ((double)x + R), dy = pcy - ((double)y + R);
+    const dfl two_pi = df_split(2.0 * M_PI), pi = df_split(M_PI);
+    dfl cl = df_add(df_atan2(dy, dx, a.sctab), dfl{thf, 0.f});
+    // Python's % with a positive divisor (collision turns may have left the orientation a
+    // little outside [0, 2 pi]: a few wraps at most)
+    for (int k2 = 0; k2 < 4 && df_sign(cl) < 0; ++k2) cl = df_add(cl, two_pi);
+    for (int k2 = 0; k2 < 4 && df_sign(df_sub(cl, two_pi)) >= 0; ++k2) cl = df_sub(cl, two_pi);
+    const dfl tn = df_add(dfl{thf, 0.f}, df_mul(df_sub(cl, pi), df_split(0.02)));
+    return (float)((double)tn.hi + (double)tn.lo);
+}
+
+// with_turn: the members' turn towards the centre is applied here (otherwise by other warps).
+__device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed, int *mq,
+                           bool with_turn) {
+    const int lane = threadIdx.x & 31;
+    const double R = a.p.agent_radius;
     const double want = a.p.consumption > a.pt.quality[k] ? a.pt.quality[k] : a.p.consumption;
     double left = a.pt.left[k];
     int D = INT_MAX;       // agent index of the member that empties the patch
@@ -179,18 +197,7 @@ __device__ void patch_loop(const ForageArgs &a, int k, bool *destroyed, int *mq)
     //     free: they are independent given D) and run 32 at a time, so the FP64 turn below is
     //     issued once per 32 members rather than once per 32 agents.
     auto member = [&](int i) {
-        // bias_agent_towards_res_center (sims.py:544-552): orientation += ((atan2 + orientation)
-        // % 2 pi - pi) * 0.02, in double-float (within ~1e-14 of FP64 before the float32 store)
-        const double dx = pcx - ((double)a.ag.x[i] + R), dy = pcy - ((double)a.ag.y[i] + R);
-        const float thf = a.ag.theta[i];
-        const dfl two_pi = df_split(2.0 * M_PI), pi = df_split(M_PI);
-        dfl cl = df_add(df_atan2(dy, dx, a.sctab), dfl{thf, 0.f});
-        // Python's % with a positive divisor (collision turns may have left the orientation a
-        // little outside [0, 2 pi]: a few wraps at most)
-        for (int k2 = 0; k2 < 4 && df_sign(cl) < 0; ++k2) cl = df_add(cl, two_pi);
-        for (int k2 = 0; k2 < 4 && df_sign(df_sub(cl, two_pi)) >= 0; ++k2) cl = df_sub(cl, two_pi);
-        const dfl tn = df_add(dfl{thf, 0.f}, df_mul(df_sub(cl, pi), df_split(0.02)));
-        a.ag.theta[i] = (float)((double)tn.hi + (double)tn.lo);
+        if (with_turn) a.ag.theta[i] = turned_orientation(a, k, a.ag.x[i], a.ag.y[i], a.ag.theta[i]);
         if (i > D) {
             notify(a, i, -1, -1);
             notify(a, i, -1, -1);
@@ -424,12 +431,25 @@ __global__ void __launch_bounds__(kResourceThreads) forage_resource_kernel(Forag
     }
     for (int k = tid; k < s.np; k += blockDim.x) destroyed[k] = 0;
     __syncthreads();
-    // 2. each patch's agents in agent order (one warp per patch: the loop is sequential)
-    for (int k = warp; k < s.np; k += nw) {
-        if (s.pt.id[k] < 0) continue;   // warp-uniform
-        bool d = false;
-        patch_loop(s, k, &d, mqueue[warp]);
-        if (lane == 0) destroyed[k] = d ? 1 : 0;
+    // 2. each patch's agents in agent order (one warp per patch: the loop is sequential).
+    //    When the state is staged and warps are left over, those warps apply the members'
+    //    turn towards the patch centre meanwhile: it reads the positions before any teleport
+    //    (still in global memory until the write-back) and only the member's orientation,
+    //    which nothing else in this phase touches.
+    const bool turn_apart = staged && s.np < nw;   // block-uniform
+    if (warp < s.np || !turn_apart) {
+        for (int k = warp; k < s.np; k += nw) {
+            if (s.pt.id[k] < 0) continue;   // warp-uniform
+            bool d = false;
+            patch_loop(s, k, &d, mqueue[warp], !turn_apart);
+            if (lane == 0) destroyed[k] = d ? 1 : 0;
+        }
+    } else {
+        for (int i = (warp - s.np) * 32 + lane; i < s.n; i += (nw - s.np) * 32) {
+            const int k = s.patch_of[i];
+            if (k >= 0 && s.pt.id[k] >= 0)
+                s.ag.theta[i] = turned_orientation(s, k, a.ag.x[i], a.ag.y[i], s.ag.theta[i]);
+        }
     }
     __syncthreads();
     // 3. emptied patches are killed and regenerated in patch order (kill_resource)
