@@ -117,6 +117,11 @@ class AbmForageRecording(ctypes.Structure):
     _fields_ = [("capacity", c_int32), ("step", c_i32_p)] + list(RECORDING_FIELDS)
 
 
+class AbmVfRecording(ctypes.Structure):
+    _fields_ = [("capacity", c_int32), ("step", c_i32_p), ("posx", c_i32_p), ("posy", c_i32_p),
+                ("orientation", c_float_p), ("velocity", c_float_p), ("vpf_bits", c_u32_p)]
+
+
 class AbmForagerState(ctypes.Structure):
     _fields_ = list(FORAGER_FIELDS)
 
@@ -184,6 +189,9 @@ SIGNATURES = [
     ("abm_vpf_get_step_split", c_int32, [c_i32_p]),
     ("abm_vpf_polarisation", c_int32,
      [c_float_p, c_int32, c_i32_p, c_int32, c_double_p, c_int32, c_i32_p, ctypes.c_void_p]),
+    ("abm_vpf_record", c_int32,
+     [ctypes.POINTER(AbmSwarmState), c_int32, c_u32_p, c_int32, ctypes.POINTER(AbmVfRecording),
+      ctypes.c_void_p]),
     ("abm_vpf_flock_step_host", c_int32,
      [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
       ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), ctypes.c_void_p]),

@@ -75,6 +75,7 @@ class BatchedSweep:
         self._graph_chunk = 0
         self._stream = None
         self._pol = None
+        self._rec = None
 
     # ------------------------------------------------------------------ ensemble statistic
     def track_polarisation(self, capacity: int):
@@ -99,12 +100,40 @@ class BatchedSweep:
             _lib.dptr(self._pol), self._pol.shape[1], _lib.i32ptr(self._pol_step),
             ctypes.c_void_p(stream.cuda_stream)), "abm_vpf_polarisation")
 
+    # ------------------------------------------------------------------ recording
+    def record_steps(self, capacity: int, vpf: bool = False):
+        """Record every instance's state after each following step on the device
+        (abm_vpf_record over the concatenated state, captured with the step in graphs), as the
+        reference's RAM recorder does in each instance's own run (vf_sims.py:328-331), for up
+        to `capacity` steps; vpf: also each step's VPF."""
+        from .swarm import VfRecorder
+        self._rec = VfRecorder(self.lib, self.n, self.words, capacity, vpf, self.device)
+        self._graph = None   # re-capture with the recorder
+
+    def instance_recording(self, k: int) -> dict:
+        """Instance k's recorded series (posx, posy, orientation, velocity, optional vpf_bits:
+        agents x steps) and the number of steps."""
+        if self._rec is None:
+            raise RuntimeError("no recording: call record_steps first")
+        out = self._rec.series(int(self.offsets[k]), int(self.offsets[k + 1]))
+        out["steps"] = self._rec.steps()
+        return out
+
+    def save_reference_run(self, k: int, folder: str, as_zarr: bool = False, env=None,
+                           save_extracted_vfield: bool = False):
+        """Write instance k's recording as the reference writes one simulation's data (JSON,
+        or the zarr arrays of USE_ZARR_FORMAT=1, and env_params.json when `env` is given)."""
+        from .recording import save_vf_run
+        save_vf_run(folder, self.instance_recording(k), self.params.rv, as_zarr, env,
+                    save_extracted_vfield)
+
     @staticmethod
     def _state(d):
         return _lib.AbmSwarmState(_lib.fptr(d["x"]), _lib.fptr(d["y"]), _lib.fptr(d["theta"]),
                                   _lib.fptr(d["v"]))
 
     def _launch(self, src: int, stream, want_vpf=False, want_terms=False) -> int:
+        want_vpf = want_vpf or (self._rec is not None and self._rec.vpf_bits is not None)
         st_in = self._state(self._bufs[src])
         st_out = self._state(self._bufs[1 - src])
         status = self.lib.abm_vpf_flock_batched(
@@ -116,6 +145,9 @@ class BatchedSweep:
         st = _lib.check(status, "abm_vpf_flock_batched")
         if self._pol is not None:
             self._record_polarisation(self._bufs[1 - src], stream)
+        if self._rec is not None:
+            self._rec.launch(self._state(self._bufs[1 - src]), self.vpf_bits, self.params.rv,
+                             stream)
         return st
 
     def step(self, want_vpf=False, want_terms=False, stream=None) -> int:
@@ -132,6 +164,7 @@ class BatchedSweep:
         self._stream = torch.cuda.Stream(self.device)
         saved = {k: t.clone() for k, t in self._bufs[self._cur].items()}
         saved_pol = None if self._pol is None else (self._pol.clone(), self._pol_step.clone())
+        saved_rec = None if self._rec is None else self._rec.step.clone()
         # the warm-up steps overwrite the state: they start once the copies are taken
         self._stream.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(self._stream):
@@ -143,6 +176,8 @@ class BatchedSweep:
         if saved_pol is not None:   # the warm-up steps are not part of the run
             self._pol.copy_(saved_pol[0])
             self._pol_step.copy_(saved_pol[1])
+        if saved_rec is not None:   # their records are overwritten by the run's
+            self._rec.step.copy_(saved_rec)
         self._stream.wait_stream(torch.cuda.current_stream(self.device))
         g = torch.cuda.CUDAGraph()
         start = self._cur

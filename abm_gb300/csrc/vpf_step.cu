@@ -769,6 +769,42 @@ __global__ void __launch_bounds__(256) polarisation_kernel(const float *theta, i
     }
 }
 
+// One column of a visual-flocking recording.  Every block reads the column before it arrives
+// at the counter rec.step[1]; the last block to arrive advances rec.step[0] and clears step[1],
+// so no block can see the advanced column within the launch (no block waits on another).
+__global__ void __launch_bounds__(256) vf_record_kernel(abm_swarm_state s, int n,
+                                                        const uint32_t *bits, int words,
+                                                        abm_vf_recording rec) {
+    const int t = __ldcg(rec.step);
+    if (t < rec.capacity) {
+        const size_t cap = (size_t)rec.capacity;
+        const int stride = gridDim.x * blockDim.x;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const size_t o = (size_t)i * cap + t;
+            rec.posx[o] = (int)s.x[i];   // Python int(): truncation toward zero
+            rec.posy[o] = (int)s.y[i];
+            rec.orientation[o] = s.theta[i];
+            rec.velocity[o] = s.v[i];
+        }
+        if (rec.vpf_bits) {
+            const size_t total = (size_t)n * words;
+            for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total;
+                 q += stride) {
+                const size_t i = q / words, w = q % words;
+                rec.vpf_bits[(i * cap + t) * words + w] = bits[q];
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(rec.step + 1, 1) == (int)gridDim.x - 1) {
+            rec.step[1] = 0;
+            rec.step[0] = t + 1;
+        }
+    }
+}
+
 // Evaluates the in-kernel double-float cos/sin (verification hook for the tests).
 __global__ void check_sincos_kernel(const float *theta, int n, double *out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1445,6 +1481,30 @@ int abm_vpf_polarisation(const float *theta_dev, int32_t n_total, const int32_t 
     polarisation_kernel<<<n_instances, 256, 0, (cudaStream_t)stream>>>(
         theta_dev, n_total, offsets_dev, out_dev, capacity, step_dev);
     return check_cuda(cudaGetLastError(), "polarisation_kernel launch");
+}
+
+int abm_vpf_record(const abm_swarm_state *s, int32_t n_total, const uint32_t *vpf_bits_dev,
+                   int32_t rv, abm_vf_recording *rec, void *stream) {
+    const char *fn = "abm_vpf_record";
+    if (!s || !rec) return set_error(ABM_ERR_INVALID_ARG, "%s: NULL argument", fn);
+    if (n_total < 0 || rec->capacity < 0)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: negative size", fn);
+    if (!rec->step) return set_error(ABM_ERR_INVALID_ARG, "%s: NULL step counter", fn);
+    if (n_total > 0 && (!s->x || !s->y || !s->theta || !s->v || !rec->posx || !rec->posy ||
+                        !rec->orientation || !rec->velocity))
+        return set_error(ABM_ERR_INVALID_ARG, "%s: NULL state or series", fn);
+    int words = 0;
+    if (rec->vpf_bits) {
+        if (rv < 1 || rv > ABM_MAX_RV) return set_error(ABM_ERR_RV, "%s: rv=%d", fn, rv);
+        if (n_total > 0 && !vpf_bits_dev)
+            return set_error(ABM_ERR_INVALID_ARG, "%s: VPF series without the step's VPF", fn);
+        words = (rv + 31) / 32;
+    }
+    const size_t items = (size_t)n_total * (words > 1 ? words : 1);
+    const int blocks = (int)std::min<size_t>(std::max<size_t>((items + 255) / 256, 1), 1216);
+    vf_record_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(*s, n_total, vpf_bits_dev, words,
+                                                               *rec);
+    return check_cuda(cudaGetLastError(), "vf_record_kernel launch");
 }
 
 int abm_vpf_check_sincos(const float *theta_dev, int32_t n, double *out_dev, void *stream) {

@@ -24,6 +24,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from .recording import agents_dict, reference_json, resources_dict, save_reference_zarr
 
 MODES = {0: "explore", 1: "relocate", 2: "exploit", 3: "pool", 4: "collide"}
 
@@ -299,6 +300,24 @@ class ForagingSim:
             with open(os.path.join(folder, "env_params.json"), "w") as f:
                 json.dump(dict(env), f, indent=4)
 
+    def save_reference_zarr(self, folder: str, env: Optional[dict] = None,
+                            save_extracted_vfield: bool = False):
+        """Write the recording as the zarr arrays of the reference's save_ifdb_as_csv with
+        as_zar=True (ifdb.py:435-536; USE_ZARR_FORMAT=1), plus env_params.json when `env` is
+        given; save_extracted_vfield adds ag_vf, the social field rebuilt from its stored edges
+        like the reference does."""
+        import json
+        import os
+        rec = self.recording()
+        agents = agents_dict(rec, self.params.rv) if save_extracted_vfield else \
+            agents_dict({k: v for k, v in rec.items() if k != "soc_bits"}, self.params.rv)
+        names = save_reference_zarr(folder, agents, resources_dict(rec), self.params.rv,
+                                    save_extracted_vfield)
+        if env is not None:
+            with open(os.path.join(folder, "env_params.json"), "w") as f:
+                json.dump(dict(env), f, indent=4)
+        return names
+
     def _dev(self, a, dt):
         arr = np.ascontiguousarray(np.asarray(a, dt))
         if dt in (np.uint32, np.uint64):
@@ -405,60 +424,6 @@ class ForagingSim:
 
     def collected(self) -> np.ndarray:
         return self.ag["collected"].cpu().numpy()
-
-
-def _pad(number, n):
-    """ifdb.pad_to_n_digits (ifdb.py:38-52)."""
-    d = n - len(str(number))
-    return d * "0" + str(number) if d > 0 else str(number)
-
-
-def reference_json(rec: dict, rv: int):
-    """(agent_data.json, resource_data.json) text of a recording (ForagingSim.recording())
-    exactly as the reference's RAM recorder and json.dump write them (ifdb.py:55-96, :223-260,
-    :412-434): per agent its name and per-step lists, the social field stored as its rising and
-    falling edge indices in numpy's printed form; per patch id its first step, name, per-step
-    position / units left / quality and its radius."""
-    import json
-    n, steps = rec["posx"].shape
-    words = rec["soc_bits"].shape[2] if rec["soc_bits"].ndim == 3 else 0
-    agents = {}
-    for i in range(n):
-        d = {"agent_name": f"agent-{_pad(i, 2)}",
-             "posx": [int(v) for v in rec["posx"][i]], "posy": [int(v) for v in rec["posy"][i]],
-             "orientation": [float(v) for v in rec["orientation"][i]],
-             "velocity": [float(v) for v in rec["velocity"][i]],
-             "w": [float(v) for v in rec["w"][i]], "u": [float(v) for v in rec["u"][i]],
-             "Ipriv": [float(v) for v in rec["ipriv"][i]],
-             "mode": [int(v) for v in rec["mode"][i]],
-             "collectedr": [float(v) for v in rec["collected"][i]],
-             "expl_patch_id": [int(v) for v in rec["patch_id"][i]],
-             "vfield_up": [], "vfield_down": []}
-        if words:
-            by = rec["soc_bits"][i].astype("<u4").view(np.uint8).reshape(steps, -1)
-            fields = np.unpackbits(by, axis=1, bitorder="little")[:, :rv].astype(np.float64)
-            for V in fields:
-                d["vfield_up"].append(f"{np.where(np.roll(V, 1) < V)[0]}")
-                d["vfield_down"].append(f"{np.where(np.roll(V, 1) > V)[0]}")
-        agents[i] = d
-    resources = {}
-    t0 = int(rec.get("t0", 0))
-    for k in range(rec["res_id"].shape[0]):
-        for t in range(steps):
-            rid = int(rec["res_id"][k, t])
-            if rid < 0:
-                continue
-            if rid not in resources:
-                resources[rid] = {"start_time": t0 + t + 1, "end_time": None,
-                                  "res_name": f"res-{_pad(rid, 3)}", "pos_x": [], "pos_y": [],
-                                  "radius": int(rec["radius"][k]), "resc_left": [],
-                                  "quality": []}
-            r = resources[rid]
-            r["pos_x"].append(int(rec["res_posx"][k, t]))
-            r["pos_y"].append(int(rec["res_posy"][k, t]))
-            r["resc_left"].append(float(rec["res_left"][k, t]))
-            r["quality"].append(float(rec["res_quality"][k, t]))
-    return json.dumps(agents), json.dumps(resources)
 
 
 def efficiency(collected_start, collected_end, dt: float) -> np.ndarray:

@@ -194,15 +194,47 @@ class BatchedProtocol:
             out.append((p, inst))
         return out
 
-    def run(self, steps: int, seed: int = 0, chunk: int = 100, device="cuda"):
+    def run_folders(self, save_root: str):
+        """Where run() writes each configuration's data: save_root/<its SAVE_ROOT_DIR>/<the
+        stem of its .env file name>, in configuration order (the reference writes a run into
+        a time-stamped folder under SAVE_ROOT_DIR, ifdb_params.py:33-39; its ExperimentLoader
+        takes every folder of a batch, data_loader.py:459-466)."""
+        import os
+        combos = len(self.combos())
+        out = []
+        for idx, env in enumerate(self.env_configs()):
+            nb, i = divmod(idx, combos)
+            out.append(os.path.join(save_root, env["SAVE_ROOT_DIR"], f"{i}_b{nb}"))
+        return out
+
+    def run(self, steps: int, seed: int = 0, chunk: int = 100, device="cuda",
+            save_root: Optional[str] = None, as_zarr: Optional[bool] = None,
+            save_extracted_vfield: bool = False):
         """Run every configuration for `steps` steps, one BatchedSweep per group; returns the
-        final state of each configuration (dicts of numpy arrays) in configuration order."""
+        final state of each configuration (dicts of numpy arrays) in configuration order.
+
+        save_root: also record every step on the device and write each configuration's run as
+        the reference writes one simulation's data at its end (vf_sims.py:373-381: the JSON
+        files, or the zarr arrays when as_zarr — by default the configuration's
+        USE_ZARR_FORMAT —, and env_params.json with the values as its .env file holds them)
+        into the folders of run_folders(save_root)."""
         from .batched import BatchedSweep
         insts = self.instances(seed)
+        envs = self.env_configs()
+        folders = self.run_folders(save_root) if save_root is not None else None
+
+        def zarr_of(env):
+            if as_zarr is not None:
+                return bool(as_zarr)
+            return bool(int(float(env.get("USE_ZARR_FORMAT", 0))))
+
         results = [None] * len(insts)
         for members in self.groups():
             base = insts[members[0]][0]
             sweep = BatchedSweep(base, [insts[m][1] for m in members], device=device)
+            if folders is not None:
+                vpf = save_extracted_vfield or not all(zarr_of(envs[m]) for m in members)
+                sweep.record_steps(steps, vpf=vpf)
             if steps >= chunk:
                 sweep.run(steps, chunk=chunk)
             else:
@@ -210,4 +242,8 @@ class BatchedProtocol:
                     sweep.step()
             for k, m in enumerate(members):
                 results[m] = sweep.instance_state(k)
+                if folders is not None:
+                    env_json = {key: f"{val}" for key, val in envs[m].items()}
+                    sweep.save_reference_run(k, folders[m], zarr_of(envs[m]), env_json,
+                                             save_extracted_vfield)
         return results

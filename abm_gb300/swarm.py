@@ -26,6 +26,43 @@ def _dev_tensor(a, device, dtype=torch.float32):
     return t.to(device=device, dtype=dtype).contiguous()
 
 
+class VfRecorder:
+    """Device series of abm_vpf_record: n agents, `capacity` steps, optionally the VPF."""
+
+    def __init__(self, lib, n: int, words: int, capacity: int, vpf: bool, device):
+        cap = int(capacity)
+        self.lib, self.n, self.words, self.capacity = lib, n, words, cap
+        self.step = torch.zeros(2, dtype=torch.int32, device=device)
+        self.posx = torch.zeros((n, cap), dtype=torch.int32, device=device)
+        self.posy = torch.zeros((n, cap), dtype=torch.int32, device=device)
+        self.orientation = torch.zeros((n, cap), dtype=torch.float32, device=device)
+        self.velocity = torch.zeros((n, cap), dtype=torch.float32, device=device)
+        self.vpf_bits = (torch.zeros((n, cap, words), dtype=torch.int32, device=device)
+                         if vpf else None)
+        self.struct = _lib.AbmVfRecording(
+            cap, _lib.i32ptr(self.step), _lib.i32ptr(self.posx), _lib.i32ptr(self.posy),
+            _lib.fptr(self.orientation), _lib.fptr(self.velocity), _lib.u32ptr(self.vpf_bits))
+
+    def launch(self, state: "_lib.AbmSwarmState", vpf_bits, rv: int, stream):
+        _lib.check(self.lib.abm_vpf_record(
+            ctypes.byref(state), self.n,
+            _lib.u32ptr(vpf_bits) if self.vpf_bits is not None else None, int(rv),
+            ctypes.byref(self.struct), ctypes.c_void_p(stream.cuda_stream)), "abm_vpf_record")
+
+    def steps(self) -> int:
+        return min(int(self.step[0].item()), self.capacity)
+
+    def series(self, a: int = 0, b: Optional[int] = None) -> dict:
+        """Rows a:b of the recorded steps as numpy: posx, posy, orientation, velocity (rows,
+        steps) and vpf_bits (rows, steps, words) uint32 when recorded."""
+        t = self.steps()
+        out = {k: getattr(self, k)[a:b, :t].cpu().numpy()
+               for k in ("posx", "posy", "orientation", "velocity")}
+        if self.vpf_bits is not None:
+            out["vpf_bits"] = self.vpf_bits[a:b, :t].cpu().numpy().view(np.uint32)
+        return out
+
+
 class VFSwarm:
     """N visual-flocking agents of one arena, state in float32 on `device`.
 
@@ -65,6 +102,8 @@ class VFSwarm:
     def step(self, want_vpf: bool = False, want_terms: bool = False,
              stream: Optional[torch.cuda.Stream] = None) -> int:
         """Advance every agent by one timestep (one kernel launch, asynchronous)."""
+        rec = getattr(self, "_rec", None)
+        want_vpf = want_vpf or (rec is not None and rec.vpf_bits is not None)
         st_in = self._state_struct(self._cur)
         st_out = self._state_struct(self._nxt)
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
@@ -80,7 +119,32 @@ class VFSwarm:
                 _lib.fptr(self._cur["theta"]), self.n, None, 1, _lib.dptr(self._pol),
                 self._pol.shape[1], _lib.i32ptr(self._pol_step),
                 ctypes.c_void_p(s.cuda_stream)), "abm_vpf_polarisation")
+        if rec is not None:
+            rec.launch(self._state_struct(self._cur), self.vpf_bits, self.params.rv, s)
         return self.last_status
+
+    def record_steps(self, capacity: int, vpf: bool = False):
+        """Record the state after every following step on the device (abm_vpf_record), as the
+        reference's RAM recorder does each step (vf_sims.py:328-331), for up to `capacity`
+        steps; vpf: also the step's VPF (its edges go into the reference's files)."""
+        self._rec = VfRecorder(self.lib, self.n, self.words, capacity, vpf, self.device)
+
+    def recording(self) -> dict:
+        """The recorded series on the host (see VfRecorder.series) and the number of steps."""
+        if getattr(self, "_rec", None) is None:
+            raise RuntimeError("no recording: call record_steps first")
+        out = self._rec.series()
+        out["steps"] = self._rec.steps()
+        return out
+
+    def save_reference_run(self, folder: str, as_zarr: bool = False, env=None,
+                           save_extracted_vfield: bool = False):
+        """Write the recording in the reference's layout: agent_data.json / resource_data.json,
+        or the ag_*.zarr arrays (USE_ZARR_FORMAT=1), plus env_params.json when `env` is given
+        (the end of VFSimulation.start, vf_sims.py:373-381)."""
+        from .recording import save_vf_run
+        save_vf_run(folder, self.recording(), self.params.rv, as_zarr, env,
+                    save_extracted_vfield)
 
     def track_polarisation(self, capacity: int):
         """Record the swarm's polarisation (|sum (cos, sin)| / N, the reference's
@@ -95,9 +159,10 @@ class VFSwarm:
 
     def run(self, steps: int, stream=None, graph_chunk: int = 0) -> int:
         """Advance `steps` steps.  graph_chunk >= 2: one library call (abm_vpf_flock_run) that
-        replays a CUDA graph of graph_chunk steps (not with polarisation tracking); the stream
+        replays a CUDA graph of graph_chunk steps (not with polarisation tracking or recording); the stream
         must then be a non-default one.  Otherwise one abm_vpf_flock_step call per step."""
-        if graph_chunk < 2 or getattr(self, "_pol", None) is not None:
+        if (graph_chunk < 2 or getattr(self, "_pol", None) is not None
+                or getattr(self, "_rec", None) is not None):
             st = 0
             for _ in range(steps):
                 st = self.step(stream=stream)

@@ -225,6 +225,32 @@ int abm_vpf_polarisation(const float *theta_dev, int32_t n_total, const int32_t 
                          int32_t *step_dev, void *stream);
 
 /*
+ * Device-side recording of a visual-flocking run: the per-step values the reference's RAM
+ * recorder keeps for each agent (ifdb.save_agent_data_RAM, abm/monitoring/ifdb.py:55-96, called
+ * after every step by VFSimulation.step_sim, vf_sims.py:328-331): int() of the top-left
+ * position, orientation, velocity and, optionally, the step's VPF whose rising / falling edges
+ * the reference stores.  The series are agent-major, (n, capacity) and (n, capacity, words).
+ */
+typedef struct abm_vf_recording {
+    int32_t capacity;          /* steps the series hold; later steps are not recorded */
+    int32_t *step;             /* device, two int32: [0] the column of the next record,
+                                  [1] launch scratch (zero it together with [0]) */
+    int32_t *posx, *posy;      /* int() of x and y: truncation toward zero */
+    float *orientation, *velocity;
+    uint32_t *vpf_bits;        /* nullable: the bitmask abm_vpf_flock_step wrote for the step
+                                  (raw pixel order; the reference's soc_v_field is its flip) */
+} abm_vf_recording;
+
+/*
+ * Append the state s (and vpf_bits_dev when rec->vpf_bits is set; rv gives its words) to the
+ * recording at column rec->step[0], then advance the counter (one launch; graph-safe).  Call it
+ * after the step, like the reference records after the agents' update.  For a batched sweep
+ * pass the concatenated state: rows follow the agents of the instances in order.
+ */
+int abm_vpf_record(const abm_swarm_state *s, int32_t n_total, const uint32_t *vpf_bits_dev,
+                   int32_t rv, abm_vf_recording *rec, void *stream);
+
+/*
  * Allocation-free variant of abm_vpf_flock_step (no counterpart in the reference): the same
  * step, arguments, results and status codes, for callers that cannot call cudaMalloc, such as
  * code running inside another framework's memory pool, a host that has reserved all device

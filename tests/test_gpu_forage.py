@@ -187,6 +187,19 @@ def test_forage_recording_matches_states_and_graph_replay():
     assert len(ag) == 40 and len(ag["0"]["posx"]) == 200 and ag["7"]["agent_name"] == "agent-07"
     assert all(len(v["vfield_up"]) == len(v["vfield_down"]) == 200 for v in ag.values())
     assert len(rs) >= 3 and env["N"] == "40"
+    from abm_gb300.recording import read_zarr_array
+    with tempfile.TemporaryDirectory() as d:
+        names = a.save_reference_zarr(d)
+        assert "ag_posx" in names and "res_left" in names and "ag_vf" not in names
+        x = read_zarr_array(f"{d}/ag_posx.zarr")
+        coll = read_zarr_array(f"{d}/ag_collr.zarr")
+        left = read_zarr_array(f"{d}/res_left.zarr")
+    # agent id a in row a - 1 (agent 0 last), patch id p in row p - 1
+    assert np.array_equal(x, np.roll(ra["posx"], -1, axis=0).astype(np.float64))
+    assert np.array_equal(coll, np.roll(ra["collected"], -1, axis=0))
+    assert left.shape == (len(rs), 200)
+    for rid, r in rs.items():
+        assert np.array_equal(left[int(rid) - 1], r["resc_left"])
 
 
 @pytest.mark.parametrize("rv", [1200, 1201, 400])
