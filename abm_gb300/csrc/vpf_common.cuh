@@ -25,6 +25,18 @@ constexpr double kPi = 3.141592653589793;
 constexpr double kFix = 1099511627776.0;          // 2^40: fixed-point scale of the tables
 constexpr double kInvFix = 1.0 / 1099511627776.0;
 
+// Programmatic dependent launch: a kernel launched with programmatic stream serialisation may
+// be scheduled while the previous kernel on the stream drains (once every block of that kernel
+// has called allow_dependent_launch or exited); wait_primary_grid returns once the previous
+// kernel has completed and its memory is visible, so a dependent kernel touches nothing that
+// earlier work writes or reads before it.  Without such a launch both return at once.
+__device__ __forceinline__ void allow_dependent_launch() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void wait_primary_grid() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // ------------------------------------------------------------------ double-float arithmetic
 struct dfl {
     float hi, lo;

@@ -386,6 +386,8 @@ __global__ void __launch_bounds__(kResourceThreads) forage_resource_kernel(Forag
     __shared__ int mqueue[kResourceThreads / 32][64];   // per patch warp: queued members
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
     const bool staged = a.n <= kStageAgents && a.np <= kStagePatches;   // block-uniform
+    wait_primary_grid();
+    allow_dependent_launch();
     ForageArgs s = a;
     if (staged) {
         stage_in(a, s, rsmem);
@@ -492,6 +494,8 @@ constexpr int kUpdateWarps = 1;
 // One warp per agent: the lanes count the social field's pixels (coalesced word loads), lane 0
 // applies the update.
 __global__ void __launch_bounds__(32 * kUpdateWarps) forage_update_kernel(ForageArgs a) {
+    wait_primary_grid();
+    allow_dependent_launch();
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * kUpdateWarps + (threadIdx.x >> 5);
     if (i >= a.n) return;   // warp-uniform
@@ -806,6 +810,8 @@ __global__ void __launch_bounds__(kCollideBlock) forage_collide_kernel(ForageArg
     __shared__ double s_w, s_th, s_D, s_u1[2], s_sum[3], s_mean[2];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nthr = blockDim.x;
     const int i = blockIdx.x;
+    wait_primary_grid();
+    allow_dependent_launch();
     const int rv = a.p.rv;
     const double R = a.p.agent_radius;
     const bool ghost = a.p.ghost_mode != 0;
@@ -1387,8 +1393,10 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
         if ((st = allow_dynamic_smem((const void *)forage_collide_kernel, 200 * 1024,
                                      "forage_collide_kernel smem")))
             return st;
-        forage_collide_kernel<<<n, kCollideBlock, collide_smem_bytes(p->rv, n), s>>>(a);
-        if ((st = check_cuda(cudaGetLastError(), "forage_collide_kernel launch"))) return st;
+        if ((st = check_cuda(launch_pdl(forage_collide_kernel, (unsigned)n, kCollideBlock,
+                                        collide_smem_bytes(p->rv, n), s, a),
+                             "forage_collide_kernel launch")))
+            return st;
     }
     {
         const size_t smem = (n <= kStageAgents && n_patches <= kStagePatches)
@@ -1396,16 +1404,19 @@ int abm_forage_step(abm_forager_state *agents, int32_t n, abm_patch_state *patch
         if ((st = allow_dynamic_smem((const void *)forage_resource_kernel, 200 * 1024,
                                      "forage_resource_kernel smem")))
             return st;
-        forage_resource_kernel<<<1, kResourceThreads, smem, s>>>(a);
+        if ((st = check_cuda(launch_pdl(forage_resource_kernel, 1u, kResourceThreads, smem, s, a),
+                             "forage_resource_kernel launch")))
+            return st;
     }
-    if ((st = check_cuda(cudaGetLastError(), "forage_resource_kernel launch"))) return st;
     st = abm_vpf_social_fields(agents->x, agents->y, agents->theta, nullptr, p->agent_radius,
                                a.exploit, agents->patch_id, n, p->vision_range,
                                p->visual_exclusion, p->patchwise_exclusion, p->rv, p->fov0,
                                p->fov1, soc_bits_dev, diag_dev, stream);
     if (st < 0) return st;
-    forage_update_kernel<<<(n + kUpdateWarps - 1) / kUpdateWarps, 32 * kUpdateWarps, 0, s>>>(a);
-    return check_cuda(cudaGetLastError(), "forage_update_kernel launch");
+    return check_cuda(launch_pdl(forage_update_kernel, (unsigned)((n + kUpdateWarps - 1) /
+                                                                  kUpdateWarps),
+                                 32 * kUpdateWarps, 0, s, a),
+                      "forage_update_kernel launch");
 }
 
 int abm_forage_run(abm_forager_state *agents, int32_t n, abm_patch_state *patches,

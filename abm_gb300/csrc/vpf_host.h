@@ -14,6 +14,24 @@ int check_cuda(cudaError_t e, const char *what);
 // (device, kernel).
 int allow_dynamic_smem(const void *func, int bytes, const char *what);
 
+// Launch with programmatic stream serialisation (see allow_dependent_launch): the kernel must
+// call wait_primary_grid before it touches global memory that earlier work uses.
+template <typename Args>
+cudaError_t launch_pdl(void (*kern)(Args), unsigned blocks, unsigned threads, size_t smem,
+                       cudaStream_t s, const Args &a) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a);
+}
+
 // Host copies of one grid's tables (built in FP64 / long double).
 struct GridHostTables {
     GridDev g;                       // device pointers unset

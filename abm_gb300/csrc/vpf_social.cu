@@ -94,6 +94,8 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
     const int tid = threadIdx.x, lane = tid & 31, nthr = blockDim.x;
     const int i = blockIdx.x;
     const int words = a.g.words, rv = a.g.rv, cap = a.cap;
+    wait_primary_grid();
+    allow_dependent_launch();
     const SocialSmem L = social_smem(words, cap);
     uint32_t *vb = reinterpret_cast<uint32_t *>(smem);
     SocialEntry *ent = reinterpret_cast<SocialEntry *>(smem + L.ent);
@@ -388,6 +390,7 @@ extern "C" int abm_vpf_social_fields(const float *x_dev, const float *y_dev,
     if ((st = allow_dynamic_smem((const void *)vpf_social_kernel, (int)smem,
                                  "vpf_social_kernel smem")))
         return st;
-    vpf_social_kernel<<<n, 32 * kSocialWarps, smem, (cudaStream_t)stream>>>(a);
-    return check_cuda(cudaGetLastError(), "vpf_social_kernel launch");
+    return check_cuda(launch_pdl(vpf_social_kernel, (unsigned)n, 32 * kSocialWarps, smem,
+                                 (cudaStream_t)stream, a),
+                      "vpf_social_kernel launch");
 }

@@ -189,17 +189,6 @@ struct QEntry<true> {
     }
 };
 
-// Programmatic dependent launch: the pair kernels let the step's second kernel launch early
-// (it is launched with programmatic stream serialisation); the second kernel prefetches the
-// step's inputs, then waits for the pair kernel's completion and memory flush before it reads
-// anything the pair kernel wrote.
-__device__ __forceinline__ void allow_dependent_launch() {
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-__device__ __forceinline__ void wait_primary_grid() {
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-
 // Transition-list capacity of a warp's drained queues (both queues, 4 B entries).
 template <bool HETERO>
 constexpr int kListCap = (kQueue + kQueue2) * (int)sizeof(QEntry<HETERO>) / 4;
