@@ -411,6 +411,7 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int words = a.g.words;
     const bool split = a.vbits != nullptr;
+    wait_primary_grid();   // the previous step's state (programmatic launch)
     const int i = a.order ? a.order[blockIdx.x] : (blockIdx.x >> a.chunk_shift);
     int j0 = a.seg_begin ? a.seg_begin[i] : 0;
     int n = a.seg_end ? a.seg_end[i] : a.n;   // neighbours are [j0, n)
@@ -506,6 +507,7 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
 
     const int i = blockIdx.x * nw + warp;
     const bool active = i < n;
+    wait_primary_grid();   // the previous step's state (programmatic launch)
     allow_dependent_launch();
     if (tid < 4) counters[tid] = 0u;
     for (int w = lane; w < words; w += 32) vb[w] = 0u;
@@ -623,6 +625,7 @@ __global__ void __launch_bounds__(64) vpf_update_kernel(const StepArgs a) {
         if (a.v0) v0 = dfl{a.v0[k], 0.f};
     }
     wait_primary_grid();
+    allow_dependent_launch();   // the next step's pair kernel waits for this one's end
     if (!live) return;
     const longlong2 *sp = reinterpret_cast<const longlong2 *>(a.sums) + 2 * (size_t)k;
     const longlong2 s0 = __ldcg(sp), s1 = __ldcg(sp + 1);
@@ -666,6 +669,7 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
             in.v0 = a.v0 ? a.v0[ku] : 0.f;
         }
         wait_primary_grid();
+        allow_dependent_launch();   // the next step's pair kernel waits for this one's end
         uint32_t *vb = reinterpret_cast<uint32_t *>(fsmem) + warp * words;
         uint32_t *gb = a.vbits + (size_t)k * words;
         for (int base = 0; base < words; base += 128) {   // loads first: one latency
@@ -867,10 +871,12 @@ static int launch_l1(StepArgs a, int wpa, int split, cudaStream_t stream, int *c
     if (c == 1) a.vbits = nullptr;
     *chunks = c;
     const unsigned blocks = (unsigned)a.n << shift;
-    if (wpa == 1) vpf_pairs_l1_kernel<TORUS, HETERO, 1><<<blocks, 32, smem, stream>>>(a);
-    else if (wpa == 2) vpf_pairs_l1_kernel<TORUS, HETERO, 2><<<blocks, 64, smem, stream>>>(a);
-    else vpf_pairs_l1_kernel<TORUS, HETERO, 4><<<blocks, 128, smem, stream>>>(a);
-    return check_cuda(cudaGetLastError(), "vpf_pairs_l1_kernel launch");
+    // programmatic launch: scheduled while the previous step's last kernel drains
+    cudaError_t e;
+    if (wpa == 1) e = launch_pdl(vpf_pairs_l1_kernel<TORUS, HETERO, 1>, blocks, 32, smem, stream, a);
+    else if (wpa == 2) e = launch_pdl(vpf_pairs_l1_kernel<TORUS, HETERO, 2>, blocks, 64, smem, stream, a);
+    else e = launch_pdl(vpf_pairs_l1_kernel<TORUS, HETERO, 4>, blocks, 128, smem, stream, a);
+    return check_cuda(e, "vpf_pairs_l1_kernel launch");
 }
 
 template <bool TORUS, bool HETERO, bool TMA>
@@ -881,8 +887,8 @@ static int launch_tiled(const StepArgs &a, int warps, cudaStream_t stream) {
     const size_t smem = tiled_smem_bytes(warps, a.tile, a.g.words, HETERO,
                                          tile_buffers(a.n, a.tile));
     const int blocks = (a.n + warps - 1) / warps;
-    kern<<<blocks, warps * 32, smem, stream>>>(a);
-    return check_cuda(cudaGetLastError(), "vpf_pairs_tiled_kernel launch");
+    return check_cuda(launch_pdl(kern, (unsigned)blocks, (unsigned)(warps * 32), smem, stream, a),
+                      "vpf_pairs_tiled_kernel launch");
 }
 
 static bool aligned16(const void *p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; }
