@@ -218,6 +218,8 @@ def save_reference_zarr(folder: str, agents: dict, resources: dict, v_field_len=
         for k in ("res_posx", "res_posy", "res_rad", "res_left", "res_qual"):
             put(k, arrs[k], (num_res, t_len))
     num_ag = len(agents)
+    if num_ag == 0:
+        raise ValueError("no agents recorded")
     t_len = len(agents[next(iter(agents))]["posx"])
     cols = {"ag_posx": "posx", "ag_posy": "posy", "ag_ori": "orientation", "ag_vel": "velocity",
             "ag_mode": "mode", "ag_w": "w", "ag_u": "u", "ag_ipriv": "Ipriv",

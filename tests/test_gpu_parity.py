@@ -343,3 +343,37 @@ def test_polarisation_ensemble_cfg0():
     pol_g, pol_o = np.array(pol_g), np.array(pol_o)
     se = np.sqrt(pol_g.var() / seeds + pol_o.var() / seeds)
     assert abs(pol_g.mean() - pol_o.mean()) < 4 * se + 1e-3, (pol_g.mean(), pol_o.mean(), se)
+
+
+@pytest.mark.parametrize("boundary", [0, 1])
+def test_single_agent_and_empty_swarm(boundary):
+    """A lone agent sees nothing (empty VPF, zero integrals) and still moves like the oracle's
+    update; a swarm of zero agents is a valid no-op of the step and of the recorder."""
+    import ctypes
+    import torch
+    from abm_gb300 import _lib
+    p = dict(gam=0.1, v0=1.0, alp0=1.0, alp1=0.08, alp2=0.0, bet0=1.0, bet1=0.08, bet2=0.0,
+             boundary=boundary, limit_movement=0, max_vel=3.0, max_th=0.1, width=500.0,
+             height=500.0, window_pad=30.0, fov0=-np.pi, fov1=np.pi, rv=1200, radius=10.0,
+             dt=1.0)
+    st = {"x": np.array([21.0]), "y": np.array([263.5]), "theta": np.array([3.0]),
+          "v": np.array([0.75])}
+    sw = _swarm_from(st, p)
+    o = st
+    for _ in range(12):   # reaches the left wall / seam
+        sw.step(want_vpf=True, want_terms=True)
+        ref = oracle.vf_step(o, p)
+        assert not sw.vpf_numpy().any()
+        _check_terms(sw.terms.cpu().numpy(), ref["terms"], "single")
+        _check_state(sw.state_numpy(), ref, "single")
+        o = {k: sw.state_numpy()[k].astype(np.float64) for k in ("x", "y", "theta", "v")}
+    lib = _lib.load()
+    empty = _lib.AbmSwarmState(None, None, None, None)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.abm_vpf_flock_step(ctypes.byref(empty), ctypes.byref(empty), 0,
+                                  ctypes.byref(sw._cparams), None, None, None, None, s) >= 0
+    step = torch.zeros(2, dtype=torch.int32, device="cuda")
+    rec = _lib.AbmVfRecording(4, _lib.i32ptr(step), None, None, None, None, None)
+    assert lib.abm_vpf_record(ctypes.byref(empty), 0, None, 1200, ctypes.byref(rec), s) == 0
+    torch.cuda.synchronize()
+    assert step.tolist() == [1, 0]
