@@ -383,6 +383,8 @@ template <typename T>
 __global__ void __launch_bounds__(32 * kEdgeWarps) edge_fwd_kernel(const EdgeArgs<T> p) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int i = blockIdx.x, lane = threadIdx.x;
+    wait_primary_grid();   // programmatic launch: the previous step's state
+    allow_dependent_launch();
     const Arcs<T> A = edge_arcs<T>(p, i, smem);
     if (threadIdx.x >= 32) return;   // integrals and update: warp 0
     T bc = 0, bs = 0, ec = 0, es = 0;
@@ -414,6 +416,8 @@ __global__ void __launch_bounds__(32 * kEdgeWarps) edge_bwd_kernel(const EdgeArg
     __shared__ T s_terms[4], s_part[3][kEdgeWarps];
     const int i = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthr = blockDim.x;
+    wait_primary_grid();   // programmatic launch: the previous step's adjoint
+    allow_dependent_launch();
     const Arcs<T> A = edge_arcs<T>(p, i, smem);
     if (warp == 0) {   // integrals: warp 0, then shared with the block
         T tb = 0, tbs = 0, te = 0, tes = 0;
@@ -556,8 +560,9 @@ static int edge_fwd(const S *in, S *out, int32_t n, const abm_vf_params *p, int3
     a.terms = terms_dev;
     st = allow_dynamic_smem((const void *)edge_fwd_kernel<T>, 200 * 1024, "edge_fwd_kernel smem");
     if (st) return st;
-    edge_fwd_kernel<T><<<n, 32 * kEdgeWarps, smem, (cudaStream_t)stream>>>(a);
-    return check_cuda(cudaGetLastError(), "edge_fwd_kernel launch");
+    return check_cuda(launch_pdl(edge_fwd_kernel<T>, (unsigned)n, 32 * kEdgeWarps, smem,
+                                 (cudaStream_t)stream, a),
+                      "edge_fwd_kernel launch");
 }
 
 template <typename T, typename S>
@@ -594,8 +599,8 @@ static int edge_bwd(const S *in, const S *grad_out, S *grad_in, double *grad_par
     }
     st = allow_dynamic_smem((const void *)edge_bwd_kernel<T>, 200 * 1024, "edge_bwd_kernel smem");
     if (st) return st;
-    edge_bwd_kernel<T><<<n, 32 * kEdgeWarps, smem, s>>>(a);
-    return check_cuda(cudaGetLastError(), "edge_bwd_kernel launch");
+    return check_cuda(launch_pdl(edge_bwd_kernel<T>, (unsigned)n, 32 * kEdgeWarps, smem, s, a),
+                      "edge_bwd_kernel launch");
 }
 
 }  // namespace abm
