@@ -253,17 +253,22 @@ __global__ void __launch_bounds__(32 * kSocialWarps) vpf_social_kernel(const Soc
     }
     __syncthreads();
     // ---- trim each interval against the strictly closer ones, in ascending order (one
-    // focal interval per thread; the closer ones read in rank order, one record each)
+    // focal interval per thread; the closer ones read in rank order, one record each).  The
+    // trimmed interval only shrinks inside the untrimmed one [s0, e0] or collapses to [0, 0],
+    // which no later step changes, so a closer interval disjoint from [s0, e0] never acts:
+    // only the intersecting ones enter the dependent chain of updates.
     for (int r = tid; r < m; r += nthr) {
         const int fe = sidx[r];
         const uint4 F = srt[r];
-        int sx = (int)F.z, ex = (int)F.w;
+        const int s0 = (int)F.z, e0 = (int)F.w;
+        int sx = s0, ex = e0;
         if (a.visual_exclusion) {
 #pragma unroll 4
             for (int q = 0; q < r; ++q) {
                 const uint4 I = srt[q];
-                if (!((I.x < F.x) || (I.x == F.x && I.y < F.y))) continue;   // strictly closer
                 const int is0 = (int)I.z, ie0 = (int)I.w;
+                const bool closer = (I.x < F.x) || (I.x == F.x && I.y < F.y);   // strictly
+                if (!(closer && is0 <= e0 && ie0 >= s0)) continue;
                 if (sx <= is0 && is0 <= ex) ex = is0;
                 if (sx <= ie0 && ie0 <= ex) sx = ie0;
                 if (is0 <= sx && ie0 >= ex) {
