@@ -189,6 +189,10 @@ SIGNATURES = [
     ("abm_vpf_get_step_split", c_int32, [c_i32_p]),
     ("abm_vpf_polarisation", c_int32,
      [c_float_p, c_int32, c_i32_p, c_int32, c_double_p, c_int32, c_i32_p, ctypes.c_void_p]),
+    ("abm_vpf_flock_run_recorded", c_int32,
+     [ctypes.POINTER(AbmSwarmState), ctypes.POINTER(AbmSwarmState), c_int32,
+      ctypes.POINTER(AbmVfParams), ctypes.POINTER(AbmAgentOverrides), c_int32, c_int32, c_u32_p,
+      ctypes.POINTER(AbmVfRecording), c_u64_p, ctypes.c_void_p]),
     ("abm_vpf_record", c_int32,
      [ctypes.POINTER(AbmSwarmState), c_int32, c_u32_p, c_int32, ctypes.POINTER(AbmVfRecording),
       ctypes.c_void_p]),

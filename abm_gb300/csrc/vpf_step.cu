@@ -1387,6 +1387,25 @@ int abm_vpf_flock_run(abm_swarm_state *a, abm_swarm_state *b, int32_t n,
     return run_steps(a, b, steps, graph_chunk, (cudaStream_t)stream, one, fn);
 }
 
+int abm_vpf_flock_run_recorded(abm_swarm_state *a, abm_swarm_state *b, int32_t n,
+                               const abm_vf_params *p, const abm_agent_overrides *ov,
+                               int32_t steps, int32_t graph_chunk, uint32_t *vpf_bits_dev,
+                               abm_vf_recording *rec, unsigned long long *diag_dev,
+                               void *stream) {
+    const char *fn = "abm_vpf_flock_run_recorded";
+    if (!a || !b || !rec) return set_error(ABM_ERR_INVALID_ARG, "%s: NULL argument", fn);
+    if (rec->vpf_bits && n > 0 && !vpf_bits_dev)
+        return set_error(ABM_ERR_INVALID_ARG, "%s: VPF series without a VPF buffer", fn);
+    uint32_t *bits = rec->vpf_bits ? vpf_bits_dev : nullptr;
+    auto one = [&](abm_swarm_state *in, abm_swarm_state *out) {
+        const int st = abm_vpf_flock_step(in, out, n, p, ov, bits, nullptr, diag_dev, stream);
+        if (st < 0) return st;
+        const int rs = abm_vpf_record(out, n, bits, p->rv, rec, stream);
+        return rs < 0 ? rs : st;
+    };
+    return run_steps(a, b, steps, graph_chunk, (cudaStream_t)stream, one, fn);
+}
+
 int abm_vpf_flock_batched_run(abm_swarm_state *a, abm_swarm_state *b, int32_t n_total,
                               const int32_t *seg_begin_dev, const int32_t *seg_end_dev,
                               const int32_t *order_dev, const abm_vf_params *p,

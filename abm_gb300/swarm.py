@@ -158,16 +158,28 @@ class VFSwarm:
         return self._pol[0, : min(steps, self._pol.shape[1])].cpu().numpy()
 
     def run(self, steps: int, stream=None, graph_chunk: int = 0) -> int:
-        """Advance `steps` steps.  graph_chunk >= 2: one library call (abm_vpf_flock_run) that
-        replays a CUDA graph of graph_chunk steps (not with polarisation tracking or recording); the stream
-        must then be a non-default one.  Otherwise one abm_vpf_flock_step call per step."""
-        if (graph_chunk < 2 or getattr(self, "_pol", None) is not None
-                or getattr(self, "_rec", None) is not None):
+        """Advance `steps` steps.  graph_chunk >= 2: one library call (abm_vpf_flock_run, or
+        abm_vpf_flock_run_recorded when recording) that replays a CUDA graph of graph_chunk
+        steps (not with polarisation tracking); the stream must then be a non-default one.
+        Otherwise one abm_vpf_flock_step call per step."""
+        rec = getattr(self, "_rec", None)
+        if graph_chunk < 2 or getattr(self, "_pol", None) is not None:
             st = 0
             for _ in range(steps):
                 st = self.step(stream=stream)
             return st
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        if rec is not None:   # step + record in the library's graph
+            status = self.lib.abm_vpf_flock_run_recorded(
+                ctypes.byref(self._state_struct(self._cur)),
+                ctypes.byref(self._state_struct(self._nxt)), self.n, ctypes.byref(self._cparams),
+                ctypes.byref(self._ov), int(steps), int(graph_chunk),
+                _lib.u32ptr(self.vpf_bits) if rec.vpf_bits is not None else None,
+                ctypes.byref(rec.struct), _lib.u64ptr(self.diag), ctypes.c_void_p(s.cuda_stream))
+            self.last_status = _lib.check(status, "abm_vpf_flock_run_recorded")
+            if steps % 2:
+                self._cur, self._nxt = self._nxt, self._cur
+            return self.last_status
         status = self.lib.abm_vpf_flock_run(
             ctypes.byref(self._state_struct(self._cur)), ctypes.byref(self._state_struct(self._nxt)),
             self.n, ctypes.byref(self._cparams), ctypes.byref(self._ov), int(steps),

@@ -251,6 +251,20 @@ int abm_vpf_record(const abm_swarm_state *s, int32_t n_total, const uint32_t *vp
                    int32_t rv, abm_vf_recording *rec, void *stream);
 
 /*
+ * abm_vpf_flock_run with the recording of every step (VFSimulation.step_sim with save_in_ram,
+ * vf_sims.py:291-331, for `steps` timesteps): each step is abm_vpf_flock_step followed by
+ * abm_vpf_record, both inside the library's graph.  vpf_bits_dev: an (n, words) device buffer
+ * for the step's VPF, needed when rec->vpf_bits is set (NULL otherwise).  Same state
+ * ping-pong, status and stream rules as abm_vpf_flock_run; results and records equal those of
+ * the same number of step + record calls.
+ */
+int abm_vpf_flock_run_recorded(abm_swarm_state *a, abm_swarm_state *b, int32_t n,
+                               const abm_vf_params *p, const abm_agent_overrides *ov,
+                               int32_t steps, int32_t graph_chunk, uint32_t *vpf_bits_dev,
+                               abm_vf_recording *rec, unsigned long long *diag_dev,
+                               void *stream);
+
+/*
  * Allocation-free variant of abm_vpf_flock_step (no counterpart in the reference): the same
  * step, arguments, results and status codes, for callers that cannot call cudaMalloc, such as
  * code running inside another framework's memory pool, a host that has reserved all device

@@ -98,3 +98,26 @@ def test_batched_recording_graph_equals_eager():
         np.testing.assert_array_equal(ra["orientation"][:, -1], finals[k]["theta"])
         np.testing.assert_array_equal(ra["posx"][:, -1],
                                       np.trunc(finals[k]["x"]).astype(np.int32))
+
+
+def test_vf_recording_in_library_graph_equals_eager():
+    """VFSwarm.run(graph_chunk) with a recorder goes through abm_vpf_flock_run_recorded (step
+    and record inside the library's graph): the same records and final state as eager steps,
+    for an even and an odd number of steps."""
+    import torch
+    for steps in (14, 15):
+        a, b = _swarm(n=300, rv=600, seed=8), _swarm(n=300, rv=600, seed=8)
+        a.record_steps(steps, vpf=True)
+        b.record_steps(steps, vpf=True)
+        for _ in range(steps):
+            a.step()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())   # b's state was set up there
+        b.run(steps, stream=s, graph_chunk=4)
+        s.synchronize()
+        ra, rb = a.recording(), b.recording()
+        assert ra["steps"] == rb["steps"] == steps
+        for key in ("posx", "posy", "orientation", "velocity", "vpf_bits"):
+            np.testing.assert_array_equal(ra[key], rb[key], err_msg=key)
+        for key, val in a.state_numpy().items():
+            np.testing.assert_array_equal(val, b.state_numpy()[key], err_msg=key)
