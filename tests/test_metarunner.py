@@ -51,6 +51,14 @@ def test_env_configs_batches_files_and_groups():
     assert envs[0]["ENV_WIDTH"] == "400" and float(envs[1]["VF_BET0"]) == 1.0
     names = [n for n, _ in bp.env_files()]
     assert names == sorted(names) and names[0] == "0_b0.env" and "10_b0.env" in names
+    # run() writes configuration k into <root>/<its SAVE_ROOT_DIR>/<its .env file stem>
+    folders = bp.run_folders("out")
+    combos = len(cases[0]["combos"])
+    assert len(folders) == len(envs)
+    for k, (env, folder) in enumerate(zip(envs, folders)):
+        nb, i = divmod(k, combos)
+        assert folder == os.path.join("out", env["SAVE_ROOT_DIR"], f"{i}_b{nb}")
+    assert sorted(os.path.basename(f) + ".env" for f in folders) == names
     # ALP0 / BET0 / N vary per agent or instance: one batched group
     assert len(bp.groups()) == 1
     insts = bp.instances(seed=3)
