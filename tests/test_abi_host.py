@@ -117,6 +117,46 @@ def test_step_argument_validation(lib):
     assert r == _lib.ABM_ERR_INVALID_ARG
 
 
+def test_record_argument_validation(lib):
+    """The recorder and the recorded run reject invalid arguments before any CUDA call."""
+    from abm_gb300 import _lib
+    from abm_gb300.params import VFParams
+    st = _lib.AbmSwarmState()
+    step = (ctypes.c_int32 * 2)()
+    sp = ctypes.cast(step, _lib.c_i32_p)
+    rec = _lib.AbmVfRecording(4, sp, None, None, None, None, None)
+    assert lib.abm_vpf_record(None, 1, None, 64, ctypes.byref(rec), None) == _lib.ABM_ERR_INVALID_ARG
+    assert lib.abm_vpf_record(ctypes.byref(st), -1, None, 64, ctypes.byref(rec),
+                              None) == _lib.ABM_ERR_INVALID_ARG
+    # agents but no series
+    assert lib.abm_vpf_record(ctypes.byref(st), 3, None, 64, ctypes.byref(rec),
+                              None) == _lib.ABM_ERR_INVALID_ARG
+    # a VPF series without the step's VPF, and a bad Rv for it
+    buf = (ctypes.c_float * 4)()
+    fp = ctypes.cast(buf, _lib.c_float_p)
+    ibuf = (ctypes.c_int32 * 4)()
+    ip = ctypes.cast(ibuf, _lib.c_i32_p)
+    ubuf = (ctypes.c_uint32 * 4)()
+    up = ctypes.cast(ubuf, _lib.c_u32_p)
+    full = _lib.AbmSwarmState(fp, fp, fp, fp)
+    rec = _lib.AbmVfRecording(4, sp, ip, ip, fp, fp, up)
+    assert lib.abm_vpf_record(ctypes.byref(full), 1, None, 64, ctypes.byref(rec),
+                              None) == _lib.ABM_ERR_INVALID_ARG
+    assert lib.abm_vpf_record(ctypes.byref(full), 1, up, 0, ctypes.byref(rec),
+                              None) == _lib.ABM_ERR_RV
+    rec.step = None
+    assert lib.abm_vpf_record(ctypes.byref(full), 1, up, 64, ctypes.byref(rec),
+                              None) == _lib.ABM_ERR_INVALID_ARG
+    p = VFParams(rv=64).to_c()
+    assert lib.abm_vpf_flock_run_recorded(ctypes.byref(st), ctypes.byref(st), 1, ctypes.byref(p),
+                                          None, 4, 2, None, None, None,
+                                          None) == _lib.ABM_ERR_INVALID_ARG
+    rec = _lib.AbmVfRecording(4, sp, ip, ip, fp, fp, up)
+    assert lib.abm_vpf_flock_run_recorded(ctypes.byref(st), ctypes.byref(st), 1, ctypes.byref(p),
+                                          None, 4, 2, None, ctypes.byref(rec), None,
+                                          None) == _lib.ABM_ERR_INVALID_ARG
+
+
 def test_step_config_validation(lib):
     assert lib.abm_vpf_set_step_config(3, 0) < 0
     assert lib.abm_vpf_set_step_config(0, 100) < 0
