@@ -250,6 +250,9 @@ def save_vf_run(folder: str, rec: dict, rv: int, as_zarr: bool = False, env=None
     vpf_bits in raw pixel order, (n, steps[, words])) like the end of VFSimulation.start
     (vf_sims.py:373-381): save_ifdb_as_csv as JSON or zarr, and env_params.json
     (env_saver.save_env_vars) when `env` is given."""
+    if save_extracted_vfield and rec.get("vpf_bits") is None:
+        raise ValueError("save_extracted_vfield needs the VPF in the recording "
+                         "(record_steps(..., vpf=True))")
     os.makedirs(folder, exist_ok=True)
     series = vf_series(rec)
     if not as_zarr:

@@ -5,6 +5,7 @@ import json
 import os
 
 import numpy as np
+import pytest
 
 from conftest import GOLDEN
 
@@ -95,6 +96,10 @@ def test_vf_run_json_and_zarr_match_reference_writer(tmp_path):
     save_vf_run(str(tmp_path / "plain"), vf, d["rv"], as_zarr=True)
     _check_zarr_folder(str(tmp_path / "plain"),
                        {k: v for k, v in d["zarr"].items() if k != "ag_vf.zarr"})
+    no_vpf = {k: v for k, v in vf.items() if k != "vpf_bits"}
+    with pytest.raises(ValueError):
+        save_vf_run(str(tmp_path / "bad"), no_vpf, d["rv"], as_zarr=True,
+                    save_extracted_vfield=True)
 
 
 def test_zarr_v2_store_layout(tmp_path):
