@@ -33,6 +33,12 @@
  *     allocate synchronously, so make such a call before capturing a CUDA graph.  A graph
  *     captured from a stream uses that stream's workspace: do not replay it concurrently with
  *     other calls on the same stream.
+ *   - The library's kernels are programmatic dependent launches: each waits for the completion
+ *     of the previous work on the stream (griddepcontrol.wait) before it touches memory, and
+ *     lets the next kernel be scheduled early.  Ordinary launches of the caller keep plain
+ *     stream order; a kernel that the caller itself launches with programmatic stream
+ *     serialisation right after a library call must call cudaGridDependencySynchronize()
+ *     before it reads the library's results.
  */
 #ifndef ABM_VPF_H
 #define ABM_VPF_H
