@@ -12,7 +12,8 @@ already moved, VFSimulation.step_sim, vf_sims.py:291-302), acts, moves and refle
 walls (vf_agent.py:52-77).  Positions and headings start uniform from numpy's generator seeded
 per run (float32 values, the precision of the GPU state).  Saved per run: the initial state and
 the polarisation |sum_i (cos theta_i, sin theta_i)| / N after every step
-(data_loader.py:1818-1824).
+(data_loader.py:1818-1824).  vf_ensemble.npz holds the walls arena, vf_ensemble_torus.npz the
+same runs on the torus (VFAgent.teleport_infinite_arena, vf_agent.py:188-204).
 """
 from __future__ import annotations
 
@@ -38,12 +39,8 @@ def initial(seed, p):
             "theta": f32(rng.uniform(0, 2 * np.pi, N)), "v": np.zeros(N)}
 
 
-def main(ref_root):
+def play(mods, p, name):
     import make_golden
-    make_golden.install_shims(ref_root)
-    from abm.projects.visual_flocking.vf_agent.vf_agent import VFAgent
-    from abm.projects.visual_flocking.vf_contrib import vf_params
-    p = make_golden.base_params()
     seeds = np.arange(RUNS) + 500
     init = {k: np.zeros((RUNS, N)) for k in ("x", "y", "theta")}
     pol = np.zeros((RUNS, T))
@@ -54,12 +51,22 @@ def main(ref_root):
         for k in init:
             init[k][r] = st[k]
         for t in range(T):
-            st, _, _ = make_golden.ref_step((VFAgent, vf_params), p, st, radii, sequential=True)
+            st, _, _ = make_golden.ref_step(mods, p, st, radii, sequential=True)
             pol[r, t] = np.hypot(np.cos(st["theta"]).sum(), np.sin(st["theta"]).sum()) / N
-        print(f"run {r}: final polarisation {pol[r, -1]:.4f} ({time.time() - t0:.0f} s)")
-    np.savez_compressed(os.path.join(HERE, "vf_ensemble.npz"), seeds=seeds, pol=pol,
+        print(f"{name} run {r}: final polarisation {pol[r, -1]:.4f} ({time.time() - t0:.0f} s)")
+    np.savez_compressed(os.path.join(HERE, name), seeds=seeds, pol=pol,
                         params=make_golden.params_vec(p), **{f"init_{k}": v for k, v in init.items()})
-    print("vf_ensemble.npz written to", HERE)
+    print(name, "written to", HERE)
+
+
+def main(ref_root):
+    import make_golden
+    make_golden.install_shims(ref_root)
+    from abm.projects.visual_flocking.vf_agent.vf_agent import VFAgent
+    from abm.projects.visual_flocking.vf_contrib import vf_params
+    mods = (VFAgent, vf_params)
+    play(mods, make_golden.base_params(), "vf_ensemble.npz")                      # walls
+    play(mods, make_golden.base_params(boundary=1), "vf_ensemble_torus.npz")      # torus
 
 
 if __name__ == "__main__":

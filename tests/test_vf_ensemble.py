@@ -3,7 +3,7 @@ reference's own sequential loop.
 
 tests/golden/vf_ensemble.npz (make_vf_ensemble.py) holds 32 runs of the plain flocking
 workload (N=10, 500 x 500 walls, Rv=1200, 1000 steps) played by the reference's VFAgent in its
-group order, each agent seeing the agents before it already moved.  Single trajectories
+group order (vf_ensemble_torus.npz: the same on the torus), each agent seeing the agents before it already moved.  Single trajectories
 diverge from any other update order or precision, so the comparison is the run mean of the
 time-averaged polarisation over the second half (data_loader.py:1818-1824), within four
 combined standard errors.
@@ -19,8 +19,8 @@ from conftest import GOLDEN, gpu_available
 T0 = 500
 
 
-def _ref():
-    z = np.load(os.path.join(GOLDEN, "vf_ensemble.npz"))
+def _ref(name="vf_ensemble.npz"):
+    z = np.load(os.path.join(GOLDEN, name))
     p = {k: float(v) for k, v in zip(oracle.P_FIELDS, z["params"])}
     init = {k: z["init_" + k] for k in ("x", "y", "theta")}
     return z, p, init
@@ -36,10 +36,11 @@ def _close(a, b):
     assert abs(a.mean() - b.mean()) <= 4 * se, (a.mean(), b.mean(), se)
 
 
-def test_oracle_snapshot_ensemble_matches_reference_runs():
+@pytest.mark.parametrize("name", ["vf_ensemble.npz", "vf_ensemble_torus.npz"])
+def test_oracle_snapshot_ensemble_matches_reference_runs(name):
     """The oracle's snapshot step (the GPU's update order, FP64) from the same initial
-    states."""
-    z, p, init = _ref()
+    states, in the walls arena and on the torus."""
+    z, p, init = _ref(name)
     ref = z["pol"][:, T0:].mean(axis=1)
     runs, T = z["pol"].shape
     res = []
