@@ -80,6 +80,8 @@ def lib():
                                                c_int, c_d, c_d, c_d, dp, dp]
             L.orc_projection_union.argtypes = [c_d, c_d, c_int, c_d, c_d, c_d, c_d, c_int, dp,
                                                dp, c_int, c_d, c_d, dp, dp]
+            L.orc_projection_union_ex.argtypes = [c_d, c_d, c_int, c_d, c_d, c_d, c_d, c_int, dp,
+                                                  dp, c_int, c_d, c_d, dp, dp, c_d, u8p, ip]
             L.orc_dphi_v.argtypes = [dp, c_int, dp]
             L.orc_vswrm.argtypes = [c_d, dp, dp, c_int, dp, c_d, c_d, c_d, dp]
             L.orc_vf_step.argtypes = [c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp, c_int, dp, dp,
@@ -94,6 +96,11 @@ def lib():
                                                      c_int, dp, c_int, c_int, dp]
             L.orc_social_vpf.argtypes = [c_int, c_int, dp, dp, dp, dp, ip, ip, c_d, c_int, c_int,
                                          c_int, c_d, c_d, dp]
+            L.orc_projection_excuse.argtypes = [c_d, c_d, c_int, c_d, c_d, c_d, c_d, c_int, dp,
+                                                dp, c_int, c_d, c_d, c_d, c_d, c_int, u8p, ip]
+            L.orc_vf_step_ex.argtypes = [c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp, c_int, dp,
+                                         dp, dp, dp, u8p, dp, dp, c_d, u8p, ip]
+            L.orc_vf_step_ex.restype = c_int
             L.orc_np_mean.argtypes = [dp, ctypes.c_longlong, ctypes.c_longlong]
             L.orc_np_mean.restype = c_d
             _lib = L
@@ -163,20 +170,51 @@ def projection_field(fov, v_field_resolution, position, radius, orientation, obj
 
 
 def projection_union(fov, v_field_resolution, position, radius, orientation, object_positions,
-                     object_sizes=None, infinite=False, arena_width=0.0, arena_height=0.0):
+                     object_sizes=None, infinite=False, arena_width=0.0, arena_height=0.0,
+                     want_excuse=False, band=1e-9):
     """The OR of projection_field's rows in raw pixel order (calc_soc_v_proj's binarised sum,
-    unflipped) without materialising the rows, and each object's decision margin."""
+    unflipped) without materialising the rows, and each object's decision margin; with
+    want_excuse also the pixels (raw order) that objects within `band` rad of a pixel / width
+    decision boundary can flip and the number of such objects."""
     objs = _f64(np.asarray(object_positions, dtype=np.float64).reshape(-1, 2))
     n = objs.shape[0]
+    rv = int(v_field_resolution)
     sizes = None if object_sizes is None else _f64(np.asarray(object_sizes, np.float64))
-    V = np.zeros(v_field_resolution, np.float64)
+    V = np.zeros(rv, np.float64)
     marg = np.zeros(n, np.float64)
-    lib().orc_projection_union(float(fov[0]), float(fov[1]), int(v_field_resolution),
-                               float(position[0]), float(position[1]), float(radius),
-                               float(orientation), n, _dp(objs), _dp(sizes),
-                               1 if infinite else 0, float(arena_width), float(arena_height),
-                               _dp(V), _dp(marg))
+    ex = np.zeros(rv, np.uint8) if want_excuse else None
+    near = ctypes.c_int(0)
+    lib().orc_projection_union_ex(
+        float(fov[0]), float(fov[1]), rv, float(position[0]), float(position[1]),
+        float(radius), float(orientation), n, _dp(objs), _dp(sizes), 1 if infinite else 0,
+        float(arena_width), float(arena_height), _dp(V), _dp(marg), float(band),
+        None if ex is None else ex.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+        ctypes.byref(near))
+    if want_excuse:
+        return V, marg, ex, int(near.value)
     return V, marg
+
+
+def projection_excuse(fov, v_field_resolution, position, radius, orientation, object_positions,
+                      object_sizes=None, boundary_cond="walls", arena_width=None,
+                      arena_height=None, vision_range=None, band=1e-9):
+    """Per object of projection_field: the pixels (flipped, like its rows) that the object's
+    alternative pixel decisions would flip when its bearing or half angle lies within `band`
+    rad of a decision boundary, and whether it does.  Returns (n x Rv uint8, n bool)."""
+    objs = _f64(np.asarray(object_positions, dtype=np.float64).reshape(-1, 2))
+    n = objs.shape[0]
+    rv = int(v_field_resolution)
+    sizes = None if object_sizes is None else _f64(np.asarray(object_sizes, np.float64))
+    ex = np.zeros((n, rv), np.uint8)
+    near = np.zeros(n, np.int32)
+    lib().orc_projection_excuse(float(fov[0]), float(fov[1]), rv, float(position[0]),
+                                float(position[1]), float(radius), float(orientation), n,
+                                _dp(objs), _dp(sizes), 1 if boundary_cond == "infinite" else 0,
+                                float(arena_width or 0.0), float(arena_height or 0.0),
+                                float("nan") if vision_range is None else float(vision_range),
+                                float(band), 1, ex.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                near.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return ex, near.astype(bool)
 
 
 def dphi_v(V) -> np.ndarray:
@@ -200,11 +238,14 @@ def vswrm(vel, Phi, V, params, alp0=None, bet0=None, v0=None) -> np.ndarray:
 
 
 def vf_step(state, params, radii=None, alp0=None, bet0=None, v0=None, sequential=False,
-            want_vpf=True, want_terms=True, want_margins=False):
+            want_vpf=True, want_terms=True, want_margins=False, want_excuse=False, band=1e-9):
     """One step of all agents; state = dict of float arrays x, y, theta, v.
 
     Returns dict with x, y, theta, v (new), vpf (n x Rv uint8 raw order), terms (n x 6),
-    margins (n x n), phi_mismatch (bool)."""
+    margins (n x n), phi_mismatch (bool); with want_excuse also excuse (n x Rv uint8 raw
+    order: per agent the pixels its pairs within `band` rad of a pixel / width decision
+    boundary can flip, the symmetric differences of their alternative decisions) and near
+    (n: the number of such pairs per agent)."""
     x, y, th, v = (_f64(state[k]) for k in ("x", "y", "theta", "v"))
     n = len(x)
     P = params_array(params)
@@ -213,15 +254,19 @@ def vf_step(state, params, radii=None, alp0=None, bet0=None, v0=None, sequential
     vpf = np.zeros((n, rv), np.uint8) if want_vpf else None
     terms = np.zeros((n, 6), np.float64) if want_terms else None
     margins = np.full((n, n), np.inf) if want_margins else None
+    excuse = np.zeros((n, rv), np.uint8) if want_excuse else None
+    near = np.zeros(n, np.int32) if want_excuse else None
     r = _f64(radii)
     a0, b0, vv0 = _f64(alp0), _f64(bet0), _f64(v0)
-    mism = lib().orc_vf_step(
+    u8 = lambda a: None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    mism = lib().orc_vf_step_ex(
         n, _dp(x), _dp(y), _dp(th), _dp(v), _dp(r), _dp(P), _dp(a0), _dp(b0), _dp(vv0),
         1 if sequential else 0, _dp(out["x"]), _dp(out["y"]), _dp(out["theta"]),
-        _dp(out["v"]),
-        None if vpf is None else vpf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
-        _dp(terms), _dp(margins))
+        _dp(out["v"]), u8(vpf), _dp(terms), _dp(margins), float(band), u8(excuse),
+        None if near is None else near.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
     out.update(vpf=vpf, terms=terms, margins=margins, phi_mismatch=bool(mism))
+    if want_excuse:
+        out.update(excuse=excuse, near=near)
     return out
 
 

@@ -144,15 +144,18 @@ static double decision_margin(const double *phis, int Rv, int t, double ca, doub
     return m;
 }
 
-/* The runs one object contributes to the raw (unflipped) row: up to three [a, b) slices in
- * numpy slice semantics; returns the number written (0 when the object is skipped or not
- * visible).  Shared by the dense-row and the union forms below. */
-static int projection_runs(const double *phis, int Rv, int f0, int f1, double acx, double acy,
-                           double v1x, double v1y, double px, double py, double ox, double oy,
-                           double size, int infinite, double W, double H, double vision_range,
-                           long long runs[6], double *margin)
+/* The pixel decisions of one object (vf_supcalc.py:55-117): the bearing `ca`, the half visual
+ * angle `half` = vis / 2, the nearest linspace pixel t and h = floor(proj_size / 2).  Returns 0
+ * when the object is skipped (same top-left position, :57-58, or beyond vision_range). */
+typedef struct {
+    double ca, half;
+    long long t, h;
+} PairDecision;
+
+static int pair_decision(const double *phis, int Rv, double acx, double acy, double v1x,
+                         double v1y, double px, double py, double ox, double oy, double size,
+                         int infinite, double W, double H, double vision_range, PairDecision *d)
 {
-    if (margin) *margin = INFINITY;
     if (ox == px && oy == py) return 0;
     double ocx = ox + size, ocy = oy + size;
     double v2x = ocx - acx, v2y = ocy - acy;
@@ -175,9 +178,19 @@ static int projection_runs(const double *phis, int Rv, int f0, int f1, double ac
     double vis = 2 * atan(size / (1 * dist));
     int t = orc_find_nearest(phis, Rv, ca);
     double ps = (vis / (2 * ORC_PI)) * Rv;
-    long long s = (long long)((double)t - floor(ps / 2));
-    long long e = (long long)((double)t + floor(ps / 2));
-    if (margin) *margin = decision_margin(phis, Rv, t, ca, vis / 2);
+    d->ca = ca;
+    d->half = vis / 2;
+    d->t = t;
+    d->h = (long long)floor(ps / 2);
+    return 1;
+}
+
+/* The runs a decision (t, h) contributes to the raw (unflipped) row (vf_supcalc.py:114-129):
+ * up to three [a, b) slices in numpy slice semantics; returns the number written (0 when the
+ * projection is not visible). */
+static int runs_of(int Rv, int f0, int f1, long long t, long long h, long long runs[6])
+{
+    long long s = t - h, e = t + h;
     int nr = 0;
     if ((f0 < s && s < f1) || (f0 < e && e < f1)) {
         if (s < 0) { runs[2 * nr] = Rv + s; runs[2 * nr + 1] = Rv; ++nr; s = 0; }
@@ -187,14 +200,79 @@ static int projection_runs(const double *phis, int Rv, int f0, int f1, double ac
     return nr;
 }
 
+/* The runs one object contributes to the raw (unflipped) row and its decision margin (both
+ * used by the dense-row and the union forms below). */
+static int projection_runs(const double *phis, int Rv, int f0, int f1, double acx, double acy,
+                           double v1x, double v1y, double px, double py, double ox, double oy,
+                           double size, int infinite, double W, double H, double vision_range,
+                           long long runs[6], double *margin)
+{
+    if (margin) *margin = INFINITY;
+    PairDecision d;
+    if (!pair_decision(phis, Rv, acx, acy, v1x, v1y, px, py, ox, oy, size, infinite, W, H,
+                       vision_range, &d))
+        return 0;
+    if (margin) *margin = decision_margin(phis, Rv, (int)d.t, d.ca, d.half);
+    return runs_of(Rv, f0, f1, d.t, d.h, runs);
+}
+
+static void fill_runs_u8(uint8_t *row, int Rv, const long long runs[6], int nr)
+{
+    for (int r = 0; r < nr; ++r) {
+        long long a = runs[2 * r], b = runs[2 * r + 1];
+        if (a < 0) { a += Rv; if (a < 0) a = 0; }      /* numpy slice semantics */
+        if (b < 0) { b += Rv; if (b < 0) b = 0; }
+        if (a > Rv) a = Rv;
+        if (b > Rv) b = Rv;
+        for (long long k = a; k < b; ++k) row[k] = 1;
+    }
+}
+
+/* Pixels (raw order) that a pair within `band` rad of a decision boundary can flip: the
+ * symmetric differences between the row of the decision taken and the rows of its
+ * alternatives -- t moved across a midpoint (or across the +-pi seam, pixel 0 <-> Rv-1) that
+ * the bearing lies within `band` of, h moved across a floor(proj_size/2) switch that the half
+ * angle lies within `band` of, and both.  OR-ed into `excuse` (Rv bytes); `work` holds 2 Rv
+ * bytes of scratch.  Returns 1 when the pair is near a boundary. */
+static int pair_alternatives(const double *phis, int Rv, int f0, int f1, const PairDecision *d,
+                             double band, uint8_t *excuse, uint8_t *work)
+{
+    long long ts[3] = {d->t, -1, -1}, hs[3] = {d->h, -1, -1};
+    int nt = 1, nh = 1;
+    const long long t = d->t;
+    if (t + 1 < Rv && fabs(d->ca - 0.5 * (phis[t] + phis[t + 1])) < band) ts[nt++] = t + 1;
+    if (t >= 1 && fabs(d->ca - 0.5 * (phis[t - 1] + phis[t])) < band) ts[nt++] = t - 1;
+    if (ORC_PI - fabs(d->ca) < band && (t == 0 || t == Rv - 1) && nt < 3)
+        ts[nt++] = Rv - 1 - t;
+    const double unit = 2 * ORC_PI / Rv;
+    if (d->h >= 1 && fabs(d->half - (double)d->h * unit) < band) hs[nh++] = d->h - 1;
+    if (fabs((double)(d->h + 1) * unit - d->half) < band) hs[nh++] = d->h + 1;
+    if (nt == 1 && nh == 1) return 0;
+    uint8_t *a = work, *b = work + Rv;
+    long long runs[6];
+    memset(a, 0, (size_t)Rv);
+    fill_runs_u8(a, Rv, runs, runs_of(Rv, f0, f1, d->t, d->h, runs));
+    for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < nh; ++j) {
+            if (i == 0 && j == 0) continue;
+            memset(b, 0, (size_t)Rv);
+            fill_runs_u8(b, Rv, runs, runs_of(Rv, f0, f1, ts[i], hs[j], runs));
+            for (int k = 0; k < Rv; ++k) excuse[k] |= (uint8_t)(a[k] ^ b[k]);
+        }
+    return 1;
+}
+
 /* OR of all objects' rows in raw pixel order (calc_soc_v_proj's sum + binarise,
- * vf_agent.py:233-236, without materialising the n x Rv rows). */
-void orc_projection_union(double fov0, double fov1, int Rv, double px, double py, double radius,
-                          double orientation, int n, const double *obj_xy,
-                          const double *obj_sizes, int infinite, double W, double H,
-                          double *V, double *margins)
+ * vf_agent.py:233-236, without materialising the n x Rv rows).  excuse (nullable, Rv bytes):
+ * the pixels that objects within `band` rad of a decision boundary can flip
+ * (pair_alternatives), their count in *near. */
+void orc_projection_union_ex(double fov0, double fov1, int Rv, double px, double py,
+                             double radius, double orientation, int n, const double *obj_xy,
+                             const double *obj_sizes, int infinite, double W, double H, double *V,
+                             double *margins, double band, uint8_t *excuse, int *near)
 {
     double *phis = (double *)malloc(sizeof(double) * (size_t)Rv);
+    uint8_t *work = excuse ? (uint8_t *)malloc(2 * (size_t)Rv) : NULL;
     orc_linspace(-ORC_PI, ORC_PI, Rv, phis);
     int f0 = orc_find_nearest(phis, Rv, fov0), f1 = orc_find_nearest(phis, Rv, fov1);
     double acx = px + radius, acy = py + radius;
@@ -202,14 +280,33 @@ void orc_projection_union(double fov0, double fov1, int Rv, double px, double py
     double aey = py + (1 - sin(orientation)) * radius;
     double v1x = aex - acx, v1y = aey - acy;
     for (int k = 0; k < Rv; ++k) V[k] = 0.0;
+    if (excuse) memset(excuse, 0, (size_t)Rv);
+    int cnt = 0;
     for (int i = 0; i < n; ++i) {
         long long runs[6];
-        int nr = projection_runs(phis, Rv, f0, f1, acx, acy, v1x, v1y, px, py, obj_xy[2 * i],
-                                 obj_xy[2 * i + 1], obj_sizes ? obj_sizes[i] : radius, infinite,
-                                 W, H, NAN, runs, margins ? &margins[i] : NULL);
+        PairDecision d;
+        if (margins) margins[i] = INFINITY;
+        if (!pair_decision(phis, Rv, acx, acy, v1x, v1y, px, py, obj_xy[2 * i],
+                           obj_xy[2 * i + 1], obj_sizes ? obj_sizes[i] : radius, infinite, W, H,
+                           NAN, &d))
+            continue;
+        if (margins) margins[i] = decision_margin(phis, Rv, (int)d.t, d.ca, d.half);
+        int nr = runs_of(Rv, f0, f1, d.t, d.h, runs);
         for (int r = 0; r < nr; ++r) np_fill(V, Rv, runs[2 * r], runs[2 * r + 1], 1.0);
+        if (excuse) cnt += pair_alternatives(phis, Rv, f0, f1, &d, band, excuse, work);
     }
+    if (near) *near = cnt;
+    free(work);
     free(phis);
+}
+
+void orc_projection_union(double fov0, double fov1, int Rv, double px, double py, double radius,
+                          double orientation, int n, const double *obj_xy,
+                          const double *obj_sizes, int infinite, double W, double H,
+                          double *V, double *margins)
+{
+    orc_projection_union_ex(fov0, fov1, Rv, px, py, radius, orientation, n, obj_xy, obj_sizes,
+                            infinite, W, H, V, margins, 0.0, NULL, NULL);
 }
 
 /*
@@ -245,6 +342,46 @@ void orc_projection_field(double fov0, double fov1, int Rv, double px, double py
         for (int k = 0; k < Rv; ++k) out[(size_t)i * Rv + k] = raw[Rv - 1 - k];
     }
     free(raw);
+    free(phis);
+}
+
+/*
+ * Excuse rows of projection_field's objects: for every object whose pixel decisions lie
+ * within `band` rad of a boundary, the pixels its alternative decisions would flip
+ * (pair_alternatives).  per_object != 0: one row per object, flipped like projection_field's
+ * rows (n x Rv bytes); otherwise the OR over all objects in raw pixel order (Rv bytes), the
+ * mask that applies to calc_soc_v_proj's union.  near: per object, 1 when near a boundary
+ * (nullable).  Same arguments as orc_projection_field otherwise.
+ */
+void orc_projection_excuse(double fov0, double fov1, int Rv, double px, double py, double radius,
+                           double orientation, int n, const double *obj_xy,
+                           const double *obj_sizes, int infinite, double W, double H,
+                           double vision_range, double band, int per_object, uint8_t *excuse,
+                           int *near)
+{
+    double *phis = (double *)malloc(sizeof(double) * (size_t)Rv);
+    uint8_t *work = (uint8_t *)malloc(3 * (size_t)Rv);
+    uint8_t *row = work + 2 * (size_t)Rv;
+    orc_linspace(-ORC_PI, ORC_PI, Rv, phis);
+    int f0 = orc_find_nearest(phis, Rv, fov0), f1 = orc_find_nearest(phis, Rv, fov1);
+    double acx = px + radius, acy = py + radius;
+    double aex = px + (1 + cos(orientation)) * radius;
+    double aey = py + (1 - sin(orientation)) * radius;
+    double v1x = aex - acx, v1y = aey - acy;
+    if (!per_object) memset(excuse, 0, (size_t)Rv);
+    for (int i = 0; i < n; ++i) {
+        PairDecision d;
+        int nb = 0;
+        if (per_object) memset(row, 0, (size_t)Rv);
+        if (pair_decision(phis, Rv, acx, acy, v1x, v1y, px, py, obj_xy[2 * i],
+                          obj_xy[2 * i + 1], obj_sizes ? obj_sizes[i] : radius, infinite, W, H,
+                          vision_range, &d))
+            nb = pair_alternatives(phis, Rv, f0, f1, &d, band, per_object ? row : excuse, work);
+        if (near) near[i] = nb;
+        if (per_object)
+            for (int k = 0; k < Rv; ++k) excuse[(size_t)i * Rv + k] = row[Rv - 1 - k];
+    }
+    free(work);
     free(phis);
 }
 
@@ -397,7 +534,8 @@ static void agent_step(int i, int n, const double *x, const double *y, const dou
                        const double *v, const double *radii, const double *P,
                        const double *alp0_i, const double *bet0_i, const double *v0_i,
                        double *xn, double *yn, double *thn, double *vn, uint8_t *vraw,
-                       double *terms, double *margins_row, int *phi_mismatch)
+                       double *terms, double *margins_row, int *phi_mismatch, double band,
+                       uint8_t *excuse, int *near)
 {
     int Rv = (int)P[P_RV];
     double R = radii ? radii[i] : P[P_RADIUS];
@@ -415,8 +553,8 @@ static void agent_step(int i, int n, const double *x, const double *y, const dou
     }
     /* calc_soc_v_proj (vf_agent.py:216-237): sum of the flipped rows, binarised; VSWRM gets
      * np.flip of that field, i.e. the OR of the rows in raw pixel order. */
-    orc_projection_union(P[P_FOV0], P[P_FOV1], Rv, x[i], y[i], R, th[i], m, objs, sizes,
-                         P[P_BOUNDARY] != 0, P[P_W], P[P_H], V, marg);
+    orc_projection_union_ex(P[P_FOV0], P[P_FOV1], Rv, x[i], y[i], R, th[i], m, objs, sizes,
+                            P[P_BOUNDARY] != 0, P[P_W], P[P_H], V, marg, band, excuse, near);
     if (vraw)
         for (int k = 0; k < Rv; ++k) vraw[k] = V[k] > 0;
     if (margins_row) {
@@ -457,13 +595,16 @@ static void agent_step(int i, int n, const double *x, const double *y, const dou
  * agents.update at :302).  sequential = 1 reproduces pygame's Group.update order (agent i
  * sees the already-moved positions of agents < i); sequential = 0 is the snapshot (Jacobi)
  * form that the GPU kernels implement.  vraw: n x Rv bytes (nullable); terms: n x 6
- * (nullable); margins: n x n decision margins (nullable).  Returns 1 when len(PHI) != Rv.
+ * (nullable); margins: n x n decision margins (nullable); excuse: n x Rv bytes (nullable),
+ * per agent the pixels (raw order) that its pairs within `band` rad of a pixel / width
+ * decision boundary can flip, with the number of such pairs in near[i].  Returns 1 when
+ * len(PHI) != Rv.
  */
-int orc_vf_step(int n, const double *x, const double *y, const double *th, const double *v,
-                const double *radii, const double *P, const double *alp0_i,
-                const double *bet0_i, const double *v0_i, int sequential, double *x_out,
-                double *y_out, double *th_out, double *v_out, uint8_t *vraw, double *terms,
-                double *margins)
+int orc_vf_step_ex(int n, const double *x, const double *y, const double *th, const double *v,
+                   const double *radii, const double *P, const double *alp0_i,
+                   const double *bet0_i, const double *v0_i, int sequential, double *x_out,
+                   double *y_out, double *th_out, double *v_out, uint8_t *vraw, double *terms,
+                   double *margins, double band, uint8_t *excuse, int *near)
 {
     int Rv = (int)P[P_RV];
     int mismatch = 0;
@@ -480,7 +621,8 @@ int orc_vf_step(int n, const double *x, const double *y, const double *th, const
             double a, b, c, d;
             agent_step(i, n, cx, cy, ct, cv, radii, P, alp0_i, bet0_i, v0_i, &a, &b, &c, &d,
                        vraw ? vraw + (size_t)i * Rv : NULL, terms ? terms + 6 * (size_t)i : NULL,
-                       margins ? margins + (size_t)i * n : NULL, &mismatch);
+                       margins ? margins + (size_t)i * n : NULL, &mismatch, band,
+                       excuse ? excuse + (size_t)i * Rv : NULL, near ? near + i : NULL);
             cx[i] = a; cy[i] = b; ct[i] = c; cv[i] = d;
         }
         memcpy(x_out, cx, sizeof(double) * (size_t)n);
@@ -495,11 +637,22 @@ int orc_vf_step(int n, const double *x, const double *y, const double *th, const
             agent_step(i, n, x, y, th, v, radii, P, alp0_i, bet0_i, v0_i, &x_out[i], &y_out[i],
                        &th_out[i], &v_out[i], vraw ? vraw + (size_t)i * Rv : NULL,
                        terms ? terms + 6 * (size_t)i : NULL,
-                       margins ? margins + (size_t)i * n : NULL, &mm);
+                       margins ? margins + (size_t)i * n : NULL, &mm, band,
+                       excuse ? excuse + (size_t)i * Rv : NULL, near ? near + i : NULL);
             mismatch |= mm;
         }
     }
     return mismatch;
+}
+
+int orc_vf_step(int n, const double *x, const double *y, const double *th, const double *v,
+                const double *radii, const double *P, const double *alp0_i,
+                const double *bet0_i, const double *v0_i, int sequential, double *x_out,
+                double *y_out, double *th_out, double *v_out, uint8_t *vraw, double *terms,
+                double *margins)
+{
+    return orc_vf_step_ex(n, x, y, th, v, radii, P, alp0_i, bet0_i, v0_i, sequential, x_out,
+                          y_out, th_out, v_out, vraw, terms, margins, 0.0, NULL, NULL);
 }
 
 /* Snapshot step restricted to focal agents [i0, i1) (the bounded CPU-baseline sample). */
@@ -512,7 +665,7 @@ int orc_vf_step_range(int n, int i0, int i1, const double *x, const double *y, c
     for (int i = i0; i < i1; ++i) {
         int mm = 0;
         agent_step(i, n, x, y, th, v, radii, P, NULL, NULL, NULL, &x_out[i], &y_out[i],
-                   &th_out[i], &v_out[i], NULL, NULL, NULL, &mm);
+                   &th_out[i], &v_out[i], NULL, NULL, NULL, &mm, 0.0, NULL, NULL);
         mismatch |= mm;
     }
     return mismatch;

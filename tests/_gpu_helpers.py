@@ -1,7 +1,9 @@
-"""Helpers shared by the GPU parity tests (seeded swarms, excused-pixel masks)."""
+"""Helpers shared by the GPU parity tests (seeded swarms, the VPF check with its excuse mask)."""
 import numpy as np
 
-import oracle
+# Pixels of pairs whose edge angle lies within this many radians of a pixel / width decision
+# boundary may differ from the reference (the FP32 / double-float decision against FP64).
+NEAR_BAND = 1e-9
 
 
 def f32(a):
@@ -20,23 +22,22 @@ def seeded_swarm(seed, n, W, H, pad=30.0, R=10.0, kappa=None, vmax=1.5):
     return {"x": x, "y": y, "theta": th, "v": v}
 
 
-def excused_pixels(margins_row, state, i, params, radii=None, band=1e-9):
-    """Pixels that a pair within `band` rad of a decision boundary can touch (either
-    decision): the union of [t-h-2, t+h+2] (with wrap) of those pairs, via the oracle."""
-    rv = int(params["rv"])
-    mask = np.zeros(rv, bool)
-    js = np.where(margins_row < band)[0]
-    for j in js:
-        objs = np.array([[state["x"][j], state["y"][j]]])
-        sz = None if radii is None else [radii[j]]
-        R = params["radius"] if radii is None else radii[i]
-        row = oracle.projection_field((params["fov0"], params["fov1"]), rv,
-                                      [state["x"][i], state["y"][i]], R, state["theta"][i],
-                                      objs, sz, "infinite" if params["boundary"] else "walls",
-                                      params["width"], params["height"])[0][::-1]
-        on = np.where(row > 0)[0]
-        for k in on:
-            mask[np.arange(k - 2, k + 3) % rv] = True
-        if len(on) == 0:
-            mask[:] = True  # a dropped projection could have appeared anywhere near it
-    return mask
+def check_vpf(gpu_vpf, want_vpf, excuse, near, what):
+    """VPF bits exact, except pixels in the oracle's excuse mask: the pixels that pairs within
+    NEAR_BAND rad of a decision boundary flip under their alternative decisions (never a whole
+    row).  Returns (mismatched pixels, agents with a mismatch, near-boundary pairs); every
+    agent with a mismatch has at least one near-boundary pair."""
+    gpu_vpf = np.asarray(gpu_vpf, np.uint8)
+    want_vpf = np.asarray(want_vpf, np.uint8)
+    bad = gpu_vpf != want_vpf
+    unexcused = bad & (np.asarray(excuse) == 0)
+    if np.any(unexcused):
+        rows = np.where(unexcused.any(axis=-1))[0] if unexcused.ndim > 1 else [0]
+        r = rows[0]
+        px = np.where(unexcused[r] if unexcused.ndim > 1 else unexcused)[0]
+        raise AssertionError(f"{what}: VPF differs outside the excuse mask: agent {r}, "
+                             f"pixels {px[:10]} ({int(unexcused.sum())} pixels in all)")
+    bad_rows = int(bad.any(axis=-1).sum()) if bad.ndim > 1 else int(bad.any())
+    n_near = int(np.sum(near))
+    assert bad_rows <= n_near, (what, bad_rows, n_near)
+    return int(bad.sum()), bad_rows, n_near
