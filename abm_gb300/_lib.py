@@ -218,6 +218,8 @@ SIGNATURES = [
       ctypes.POINTER(AbmStepConfig), ctypes.POINTER(AbmStepConfig), c_int32, c_i32_p,
       ctypes.c_void_p]),
     ("abm_vpf_check_sincos", c_int32, [c_float_p, c_int32, c_double_p, c_void_p]),
+    ("abm_vpf_status", c_int32, [c_int32, c_void_p]),
+    ("abm_vpf_debug_wait_timeout", c_int32, [c_int32, c_u64_p, c_i32_p, c_void_p]),
     ("abm_probe_pipe_peak", c_int32,
      [c_int32, c_int32, c_int32, c_int32, c_float_p, c_double_p, c_void_p]),
 ]

@@ -764,10 +764,13 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
-// Bounded wait on an mbarrier phase; false when the limit was reached.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase: at most `polls` try_wait rounds; false when the limit was
+// reached (the phase has not completed).
+constexpr int kMbarPolls = 1 << 20;
+
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int polls = kMbarPolls) {
     const uint32_t addr = smem_u32(bar);
-    for (int it = 0; it < (1 << 20); ++it) {
+    for (int it = 0; it < polls; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -780,5 +783,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     }
     return false;
 }
+
+// Bit of the step kernels' status word (vpf_step.cu) set by a block whose bounded wait gave up.
+constexpr unsigned kStatusWaitTimeout = 1u;
 
 }  // namespace abm

@@ -57,6 +57,10 @@ static std::mutex g_cfg_mu;
 // cos/sin(k 2pi/1024) as double-float pairs, read with warp-uniform indices (constant cache).
 __constant__ float4 c_sincos[kSinCosTab];
 
+// Status word of the step kernels on this device (kStatusWaitTimeout: a block's bounded wait
+// gave up); read and cleared by abm_vpf_status.  A module global: no allocation.
+__device__ unsigned int g_kernel_status = 0u;
+
 static int ensure_sincos_table() {
     static std::mutex mu;
     static bool done[64] = {};
@@ -213,6 +217,7 @@ constexpr size_t kNaBytes = kNaCpt + na_round(sizeof(longlong2) * kNoAllocMaxRv)
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
 struct NoAllocDevice {
+    std::mutex mu;                   // serialises the host-side state below and its uploads
     unsigned char *base = nullptr;   // device address of g_noalloc_scratch on this device
     bool sincos_loaded = false;
     bool grid_loaded = false;        // which grid's tables the array holds
@@ -221,9 +226,9 @@ struct NoAllocDevice {
     GridDev g;
 };
 
-// Once per device (with that device current): the device address of the scratch array.
+// The current device's no-alloc record; set-up once per device (with that device current):
+// the device address of the scratch array.  Call with the record's mutex held.
 static NoAllocDevice *noalloc_device(int *status) {
-    static std::mutex mu;
     static NoAllocDevice devs[64];
     int dev = 0;
     *status = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
@@ -232,17 +237,8 @@ static NoAllocDevice *noalloc_device(int *status) {
         *status = set_error(ABM_ERR_UNSUPPORTED, "device %d beyond the no-alloc table", dev);
         return nullptr;
     }
-    std::lock_guard<std::mutex> lk(mu);
-    NoAllocDevice &d = devs[dev];
-    if (!d.base) {
-        void *ptr = nullptr;
-        *status = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_scratch),
-                             "cudaGetSymbolAddress(g_noalloc_scratch)");
-        if (*status) return nullptr;
-        d.base = (unsigned char *)ptr;
-    }
     *status = ABM_OK;
-    return &d;
+    return &devs[dev];
 }
 
 // Heavy decision + rasterisation of up to 32 queued candidates (lane < cnt holds one).
@@ -546,8 +542,21 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
         if (TMA) {
             if (tid == 0 && k + 1 < ntiles) issue(k + 1);
             tn_s = tn & ~3;
-            if (tn_s > 0 && !mbar_wait(&bars[k & 1], (uint32_t)((k >> 1) & 1))) {
-                if (lane == 0) atomicAdd(&counters[2], 1u);
+            const bool ok = tn_s <= 0 || mbar_wait(&bars[k & 1], (uint32_t)((k >> 1) & 1));
+            if (__syncthreads_or(!ok)) {
+                // The tile did not arrive within the poll limit: record it, wait (bounded
+                // again) for this block's copies still in flight -- tile k and, when issued,
+                // tile k + 1 -- so none lands after the block exits, and leave without
+                // results; abm_vpf_status reports the timeout to the host.
+                if (tid == 0) {
+                    counters[2] += 1u;
+                    atomicOr(&g_kernel_status, kStatusWaitTimeout);
+                    if (k + 1 < ntiles && (min(tile, n - base - tile) & ~3) > 0)
+                        mbar_wait(&bars[(k + 1) & 1], (uint32_t)(((k + 1) >> 1) & 1));
+                    if (tn_s > 0) mbar_wait(&bars[k & 1], (uint32_t)((k >> 1) & 1));
+                    flush_counters(a, counters);
+                }
+                return;
             }
         } else {
             float *w = buf0 + (k & 1) * (nbuf - 1) * NF * tile;
@@ -807,6 +816,33 @@ __global__ void check_sincos_kernel(const float *theta, int n, double *out) {
     out[2 * k] = (double)c.hi + (double)c.lo;
     out[2 * k + 1] = (double)s.hi + (double)s.lo;
 }
+
+// Test hook of the bounded wait: an mbarrier armed for 16 bytes that no copy delivers (no bulk
+// copy is issued, so nothing is in flight when the block exits), then `polls` try_wait rounds.
+// result[0] = 1 if the wait saw the phase complete, 0 if it gave up; a give-up is counted and
+// raises the timeout status like the tiled kernel's.
+__global__ void wait_timeout_probe_kernel(int polls, unsigned long long *diag, int *result) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_expect_tx(&bar, 16);
+    __syncthreads();
+    const bool ok = mbar_wait(&bar, 0, polls);
+    const bool gave_up = __syncthreads_or(!ok);
+    if (threadIdx.x == 0) {
+        result[0] = ok ? 1 : 0;
+        if (gave_up) {
+            if (diag) atomicAdd(&diag[ABM_DIAG_TIMEOUTS], 1ull);
+            atomicOr(&g_kernel_status, kStatusWaitTimeout);
+        }
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bar)) : "memory");
+    }
+}
+
+__global__ void clear_status_kernel(unsigned bits) { atomicAnd(&g_kernel_status, ~bits); }
 
 // Launch of the step's second kernel after the pair kernel with programmatic stream
 // serialisation (it may start while the pair kernel drains; it waits in griddepcontrol.wait).
@@ -1435,8 +1471,31 @@ int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, 
                          p->rv, kNoAllocMaxRv);
     NoAllocDevice *d = noalloc_device(&st);
     if (!d) return st;
-    if ((st = ensure_sincos_table())) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    // one host thread at a time per device, from the state check through the launches
+    std::lock_guard<std::mutex> lk(d->mu);
+    const bool need_grid =
+        !d->grid_loaded || d->rv != p->rv || d->fov0 != p->fov0 || d->fov1 != p->fov1;
+    if (!d->base || !d->sincos_loaded || need_grid) {
+        // set-up copies from host memory: refused while the stream is being captured, since a
+        // captured copy would read host memory that is gone when the graph runs
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        st = check_cuda(cudaStreamIsCapturing(s, &cap), "cudaStreamIsCapturing");
+        if (st) return st;
+        if (cap != cudaStreamCaptureStatusNone)
+            return set_error(ABM_ERR_INVALID_ARG,
+                             "%s: the first call on a device and the first call for a grid "
+                             "(rv=%d, fov=[%g, %g]) copy set-up tables and must not be made "
+                             "during stream capture", fn, p->rv, p->fov0, p->fov1);
+    }
+    if (!d->base) {
+        void *ptr = nullptr;
+        st = check_cuda(cudaGetSymbolAddress(&ptr, g_noalloc_scratch),
+                        "cudaGetSymbolAddress(g_noalloc_scratch)");
+        if (st) return st;
+        d->base = (unsigned char *)ptr;
+    }
+    if ((st = ensure_sincos_table())) return st;
     if (!d->sincos_loaded) {   // set-up: the double-float sincos table into the array
         std::vector<float> tab;
         sincos_table_host(tab);
@@ -1446,8 +1505,9 @@ int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, 
         if (st) return st;
         d->sincos_loaded = true;
     }
-    if (!d->grid_loaded || d->rv != p->rv || d->fov0 != p->fov0 || d->fov1 != p->fov1) {
-        // (re)load this grid's tables into the array, ordered on the caller's stream
+    if (need_grid) {
+        // (re)load this grid's tables into the array, ordered on the caller's stream; a copy
+        // from pageable memory has read its source when it returns
         GridHostTables t;
         build_grid_host(p->rv, p->fov0, p->fov1, t);
         GridDev g = t.g;
@@ -1460,14 +1520,12 @@ int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, 
             {kNaCot2, t.cot2.data(), t.cot2.size() * sizeof(float)},
             {kNaQ, t.q.data(), t.q.size() * sizeof(long long)},
             {kNaCpt, t.cpt.data(), t.cpt.size() * sizeof(long long)}};
+        d->grid_loaded = false;
         for (const auto &pt : parts) {
             st = check_cuda(cudaMemcpyAsync(d->base + pt.off, pt.src, pt.bytes,
                                             cudaMemcpyHostToDevice, s),
                             "cudaMemcpyAsync(no-alloc tables)");
-            if (st) {
-                d->grid_loaded = false;
-                return st;
-            }
+            if (st) return st;
         }
         d->g = g;
         d->rv = p->rv;
@@ -1475,7 +1533,7 @@ int abm_vpf_flock_step_noalloc(const abm_swarm_state *in, abm_swarm_state *out, 
         d->fov1 = p->fov1;
         d->grid_loaded = true;
     }
-    Workspace na_ws;   // the one-block-per-agent form: no bitmask workspace
+    Workspace na_ws;   // no bitmask workspace: the one-block-per-agent or the tiled form
     na_ws.sums = (long long *)(d->base + kNaSums);
     return step_launch(in, out, n, p, ov, vpf_bits_dev, terms_dev, diag_dev, s, &d->g,
                        (const float4 *)(d->base + kNaSin), na_ws, fn);
@@ -1529,6 +1587,35 @@ int abm_vpf_check_sincos(const float *theta_dev, int32_t n, double *out_dev, voi
     if (st) return st;
     check_sincos_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(theta_dev, n, out_dev);
     return check_cuda(cudaGetLastError(), "check_sincos_kernel launch");
+}
+
+int abm_vpf_status(int32_t clear, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = check_cuda(cudaStreamSynchronize(s), "abm_vpf_status: cudaStreamSynchronize");
+    if (st) return st;
+    unsigned v = 0;
+    st = check_cuda(cudaMemcpyFromSymbol(&v, g_kernel_status, sizeof(v)),
+                    "abm_vpf_status: read the status word");
+    if (st) return st;
+    if (v && clear) {   // clear only the bits read, so a concurrent launch's bit survives
+        clear_status_kernel<<<1, 1, 0, s>>>(v);
+        st = check_cuda(cudaGetLastError(), "clear_status_kernel launch");
+        if (!st) st = check_cuda(cudaStreamSynchronize(s), "abm_vpf_status: clear");
+        if (st) return st;
+    }
+    if (v & kStatusWaitTimeout)
+        return set_error(ABM_ERR_TIMEOUT, "abm_vpf_status: a step kernel gave up a bounded wait "
+                                          "for its staged neighbour tile; that launch's results "
+                                          "are incomplete");
+    return ABM_OK;
+}
+
+int abm_vpf_debug_wait_timeout(int32_t polls, unsigned long long *diag_dev, int32_t *result_dev,
+                               void *stream) {
+    if (polls < 1 || polls > (1 << 20) || !result_dev)
+        return set_error(ABM_ERR_INVALID_ARG, "abm_vpf_debug_wait_timeout: polls=%d", polls);
+    wait_timeout_probe_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(polls, diag_dev, result_dev);
+    return check_cuda(cudaGetLastError(), "wait_timeout_probe_kernel launch");
 }
 
 int abm_vpf_project_rows(const double fov[2], int32_t rv, const double pos_host[2],

@@ -208,6 +208,13 @@ class VFSwarm:
         bits = np.unpackbits(words.reshape(self.n, -1), axis=1, bitorder="little")
         return bits[:, : self.params.rv]
 
+    def check_status(self, stream=None) -> None:
+        """Synchronise the stream and raise AbmError(ABM_ERR_TIMEOUT) if a step kernel on this
+        device gave up a bounded wait since the last check (abm_vpf_status; clears the flag)."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _lib.check(_lib.load().abm_vpf_status(1, ctypes.c_void_p(s.cuda_stream)),
+                   "abm_vpf_status")
+
     def diagnostics(self) -> dict:
         d = self.diag.cpu().numpy()
         return {"pairs_resolved": int(d[_lib.DIAG_PAIRS_RESOLVED]),

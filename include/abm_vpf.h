@@ -273,20 +273,22 @@ int abm_vpf_flock_run_recorded(abm_swarm_state *a, abm_swarm_state *b, int32_t n
 /*
  * Allocation-free variant of abm_vpf_flock_step (no counterpart in the reference): the same
  * step, arguments, results and status codes, for callers that cannot call cudaMalloc, such as
- * code running inside another framework's memory pool, a host that has reserved all device
- * memory, or a graph-building layer that must not change the allocation state.  Its scratch
- * (the per-agent VSWRM sums between the two launches, the lookup tables of one grid and the
- * double-float sincos table) lives in a file-scope device array of about 2.5 MiB that
- * every GPU loading the library holds until the process exits; no cudaMalloc, cudaFree or other
- * allocating routine is called.
+ * code running inside another framework's memory pool (an allocation outside the pool breaks
+ * its accounting) or a process that has reserved all device memory up front.  Its scratch (the
+ * per-agent VSWRM sums between the two launches, the lookup tables of one grid and the
+ * double-float sincos table) lives in a file-scope device array of about 2.5 MiB that every GPU
+ * loading the library holds until the process exits; no cudaMalloc, cudaFree or other
+ * allocating routine is called.  Up to 16384 agents it runs the one-block-per-agent pair
+ * kernel, above that the tiled one (neither needs the bitmask workspace of the split form).
  * Limits: n <= ABM_NOALLOC_MAX_AGENTS and rv <= ABM_NOALLOC_MAX_RV, larger values return
  * ABM_ERR_INVALID_ARG / ABM_ERR_RV with a message.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) and copies the sincos table into it, and a call
- * with a different rv or field of view copies that grid's tables (synchronously from pageable
- * memory), so make the first call, and the first call for each grid, before any stream capture.
- * Every call shares the one array and it keeps the last call's contents (nothing in it needs to
- * start at zero: each launch overwrites the sums it reads); calls that overlap on the GPU race
- * on it, so serialise them.
+ * with a different rv or field of view copies that grid's tables into it (from pageable host
+ * memory), overwriting the tables that earlier calls used; make the first call, and the first
+ * call for each grid, before any stream capture (such a call made during capture returns
+ * ABM_ERR_INVALID_ARG).  Every call shares the one array and it keeps the last call's contents
+ * (nothing in it needs to start at zero: each launch overwrites the sums it reads); calls that
+ * overlap on the GPU race on it, so serialise them.  Host threads are serialised per device.
  */
 #define ABM_NOALLOC_MAX_AGENTS 65536
 #define ABM_NOALLOC_MAX_RV 8192
@@ -425,6 +427,28 @@ int abm_vpf_autotune(const abm_swarm_state *in, int32_t n, const int32_t *seg_be
                      const abm_vf_params *p, const abm_agent_overrides *ov, int32_t reps,
                      abm_step_config *best, abm_step_config *tried, int32_t max_tried,
                      int32_t *n_tried, void *stream);
+
+/*
+ * Status of the step kernels' bounded waits (no counterpart in the reference, which has no
+ * device waits; the nearest analogue is its status-and-skip of vf_agent.py:268, :283-284).
+ * The tiled pair kernel waits for each neighbour tile that the TMA bulk engine stages, at most
+ * 2^20 polls; a block whose wait gives up waits (bounded) for its own copies still in flight,
+ * writes no results, counts the event in ABM_DIAG_TIMEOUTS and sets a device status flag.
+ * The step entry points return once their kernels are launched, so such a failure is
+ * asynchronous, like CUDA's own kernel errors: abm_vpf_status synchronises `stream`, then
+ * returns ABM_ERR_TIMEOUT if any step kernel on the current device gave up a wait since the
+ * flag was last cleared (clear != 0 clears it), else ABM_OK.  The launch that gave up left
+ * incomplete results.  No allocation.
+ */
+int abm_vpf_status(int32_t clear, void *stream);
+
+/* Test hook of the bounded wait (no counterpart in the reference): one block arms an mbarrier
+ * for 16 bytes that no copy will deliver (no bulk copy is issued) and waits at most `polls`
+ * (1 .. 2^20) try_wait rounds; result_dev[0] = 1 if the phase completed, 0 if the wait gave
+ * up.  A give-up is counted in diag_dev[ABM_DIAG_TIMEOUTS] (nullable) and sets the status that
+ * abm_vpf_status reports, exactly as in the tiled pair kernel. */
+int abm_vpf_debug_wait_timeout(int32_t polls, unsigned long long *diag_dev, int32_t *result_dev,
+                               void *stream);
 
 /* Verification hook (no counterpart in the reference): evaluates the double-float cos/sin of
  * float32 headings that the pair kernels use for the focal agent's heading vector.

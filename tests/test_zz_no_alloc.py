@@ -1,13 +1,13 @@
 """The allocation-free step entry point (abm_vpf_flock_step_noalloc) against the regular one.
 
-Some callers cannot allocate device memory (a host framework that owns the memory pool, a
-process that reserved all device memory, a graph builder that must not change allocation
-state); the no-alloc entry point serves them from a fixed file-scope scratch array.  This
-test calls both entry points through the C ABI on two calls in a row, with different swarm
-sizes and grids so the second call has to replace the array's previous contents, and checks
-that the results agree within the parity tolerances the other GPU tests use (they are in fact
-expected to be bit-identical).  It also checks the size limits.  The file name makes pytest
-collect it last.
+Some callers cannot allocate device memory (code inside a host framework that owns the device
+memory pool, a process that reserved all device memory); the no-alloc entry point serves them
+from a fixed file-scope scratch array.  This test calls both entry points through the C ABI on
+calls in a row, with different swarm sizes and grids so each call has to replace the array's
+previous contents, and checks that the results agree within the parity tolerances the other GPU
+tests use (they are in fact expected to be bit-identical).  The sizes cover both pair kernels
+the entry point uses: the one-block-per-agent form (up to 16384 agents) and the tiled form
+(above).  It also checks the size limits.  The file name makes pytest collect it last.
 """
 import ctypes
 
@@ -56,8 +56,9 @@ def test_no_alloc_matches_regular_entry_point():
     from abm_gb300.params import VFParams
     lib = _lib.load()
     rng = np.random.default_rng(77)
-    cases = [(3000, 3600, 5.0, 5000.0, "walls"), (700, 1200, 10.0, 600.0, "infinite")]
-    for n, rv, R, W, boundary in cases:   # two calls in a row, different grids and sizes
+    cases = [(3000, 3600, 5.0, 5000.0, "walls"), (700, 1200, 10.0, 600.0, "infinite"),
+             (20000, 1200, 3.0, 9000.0, "walls")]   # the last one: the tiled pair kernel
+    for n, rv, R, W, boundary in cases:   # calls in a row, different grids and sizes
         state = {"x": rng.uniform(25, W + 25, n), "y": rng.uniform(25, W + 25, n),
                  "theta": rng.uniform(0, 2 * np.pi, n), "v": rng.uniform(0, 1, n)}
         params = VFParams(alp1=0.08, bet1=0.08, width=W, height=W, rv=rv, radius=R,
