@@ -1,4 +1,4 @@
-"""Fit the FP32 arctangent polynomial used by the pair kernels (abm_vpf_math.cuh).
+"""Fit the FP32 arctangent polynomial used by the pair kernels (vpf_common.cuh).
 
 atan(r) on r in [0, 1] is approximated as r * P(r^2), P of degree DEG, by a near-minimax
 fit of the ABSOLUTE error: Lawson's iteratively reweighted least squares on a dense grid

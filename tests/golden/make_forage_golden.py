@@ -265,4 +265,8 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ABM_REFERENCE_ROOT")
+    if not root:
+        sys.exit(f"usage: python {os.path.basename(__file__)} REFERENCE_ROOT "
+                 "(or set ABM_REFERENCE_ROOT): the root of the scioip34/ABM source tree")
+    main(root)

@@ -57,14 +57,16 @@ def test_oracle_snapshot_ensemble_matches_reference_runs(name):
 
 
 @pytest.mark.gpu
-def test_gpu_ensemble_matches_reference_runs():
+@pytest.mark.parametrize("name", ["vf_ensemble.npz", "vf_ensemble_torus.npz"])
+def test_gpu_ensemble_matches_reference_runs(name):
     """256 GPU runs (the reference's 32 initial states and 224 more drawn the same way) in one
-    batched sweep with the on-device polarisation series."""
+    batched sweep with the on-device polarisation series, in the walls arena and on the
+    torus."""
     if not gpu_available():
         pytest.skip("no CUDA device")
     from abm_gb300.batched import BatchedSweep
     from abm_gb300.params import VFParams
-    z, p, init = _ref()
+    z, p, init = _ref(name)
     runs, T = z["pol"].shape
     n = init["x"].shape[1]
     insts = [{"x": init["x"][r].astype(np.float32), "y": init["y"][r].astype(np.float32),
@@ -76,7 +78,7 @@ def test_gpu_ensemble_matches_reference_runs():
                       "y": rng.uniform(pad - R, pad + W - R, n).astype(np.float32),
                       "theta": rng.uniform(0, 2 * np.pi, n).astype(np.float32)})
     vp = VFParams(alp1=p["alp1"], bet1=p["bet1"], width=W, height=p["height"], rv=int(p["rv"]),
-                  radius=R)
+                  radius=R, boundary="infinite" if p["boundary"] else "walls")
     sweep = BatchedSweep(vp, insts)
     sweep.track_polarisation(T)
     sweep.run(T, chunk=100)
