@@ -143,6 +143,9 @@ struct GridDev {
     int rv, words, f0, f1;     // f0/f1: find_nearest(phis, fov0 / fov1)
     int kmax;                  // cot2 valid for 1 <= k < kmax (2 pi k / Rv < pi / 2)
     int phi_ok;                // len(np.arange(-pi, pi, 2pi/Rv)) == Rv
+    int full_fov;              // f0 == 0 and f1 == Rv - 1: every projection with h >= 1 is
+                               // visible (vf_supcalc.py:119 can only fail when 2h >= Rv - 1,
+                               // and h < Rv / 4 since atan(R/d) < pi/2)
     float inv_delta;           // (Rv - 1) / (2 pi): linspace pixels per radian
     float half_rm1;            // (Rv - 1) / 2 (exact)
     float rvm1;                // Rv - 1
@@ -357,6 +360,44 @@ __device__ __forceinline__ PairEst estimate_pair(const FocalDev &f, float dx, fl
     return r;
 }
 
+// FP32 decisions of one live pair of equal radii from its queued offset (dx, dy) and d^2:
+// t (nearest linspace pixel of the bearing, round to nearest) and h = floor(proj_size / 2).
+// unc: a decision lies inside its guard band (the double-float re-decision takes it), the
+// bearing lies near the +-pi seam, or the discs overlap (R / d > 1, where the arctangent
+// argument leaves [0, 1]); t and h are meaningful only when unc is false, and then
+// 0 <= t < Rv.
+struct FastEst {
+    int t, h;
+    bool unc;
+};
+
+__device__ __forceinline__ FastEst estimate_fast(const FocalDev &f, float dx, float dy, float d2,
+                                                 float R, float R2, const GridDev &g) {
+    FastEst r;
+    const float rsq = rsqrt_approx(d2);
+    // (P, Q) = (c dy + s dx, c dx - s dy): cross and dot of the heading with the offset
+    const float2 PQ = __ffma2_rn(make_float2(f.c, f.c), make_float2(dy, dx),
+                                 __fmul2_rn(make_float2(f.s, -f.s), make_float2(dx, dy)));
+    const float P = PQ.x, Q = PQ.y;
+    const float ay = fabsf(P), ax = fabsf(Q);
+    const float2 rr = make_float2(fminf(ax, ay) * rcp_approx(fmaxf(ax, ay)), R * rsq);
+    const float2 at = __fmul2_rn(rr, atan_poly2(__fmul2_rn(rr, rr)));
+    float a = at.x;
+    a = (ay > ax) ? kHalfPiF - a : a;
+    a = (Q < 0.f) ? kPiF - a : a;
+    const float ca = (P >= 0.f) ? -a : a;
+    // (u, ps2): pixel coordinate of the bearing and proj_size / 2
+    const float2 up = __ffma2_rn(make_float2(ca, at.y), make_float2(g.inv_delta, g.ps2_scale),
+                                 make_float2(g.half_rm1, 0.f));
+    const float ut = rintf(up.x), hf = floorf(up.y);
+    const float2 fr = __fadd2_rn(up, make_float2(-ut, -hf - 0.5f));   // |fr.x|, |fr.y| <= 1/2
+    r.t = (int)ut;
+    r.h = (int)hf;
+    r.unc = fabsf(fr.x) > 0.5f - g.band_t || fabsf(up.x - g.half_rm1) > g.half_rm1 - g.band_t ||
+            fabsf(fr.y) > 0.5f - g.band_h * fmaxf(up.y, 1.f) || d2 < R2;
+    return r;
+}
+
 // Visibility test of vf_supcalc.py:119 (strict, on the pixel indices).
 __device__ __forceinline__ bool projection_visible(const GridDev &g, int s, int e) {
     // f0 < k < f1  <=>  (unsigned)(k - f0 - 1) < (unsigned)(f1 - f0 - 1)
@@ -369,8 +410,9 @@ __device__ __forceinline__ bool projection_visible(const GridDev &g, int s, int 
 __device__ __forceinline__ void raster_fast(uint32_t *vb, int rv, int s, int e) {
     const unsigned len = (unsigned)(e - s);
     if (s >= 0 && e < rv && len <= 32u) {
-        // run mask of `len` ones shifted to bit s & 31, split over words w0, w0 + 1
-        const uint32_t m = len >= 32u ? ABM_FULL_MASK : ((1u << len) - 1u);
+        // run mask of `len` ones (0xffffffff >> (32 - len), none for len = 0) shifted to bit
+        // s & 31, split over words w0, w0 + 1
+        const uint32_t m = __funnelshift_rc(ABM_FULL_MASK, 0u, 32u - len);
         const int w0 = s >> 5, sh = s & 31;
         const uint32_t lo = m << sh;
         const uint32_t hi = __funnelshift_l(m, 0u, sh);

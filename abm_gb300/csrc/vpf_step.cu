@@ -170,16 +170,17 @@ static void *device_view(const void *host) {
 constexpr int kQueue = 64;
 constexpr int kQueue2 = 64;
 
+// A queued candidate.  Equal radii: the pair's FP32 centre offset, d^2 and the neighbour's
+// index (so phase B starts from the offset, and the rare double-float re-decision reloads the
+// neighbour's position); per-agent radii: the neighbour's position and radius.
 template <bool HETERO>
 struct QEntry;
 template <>
 struct QEntry<false> {
-    float2 v;
-    __device__ __forceinline__ float x() const { return v.x; }
-    __device__ __forceinline__ float y() const { return v.y; }
-    __device__ __forceinline__ float r(float r0) const { return r0; }
-    __device__ __forceinline__ static QEntry make(float x, float y, float) {
-        return QEntry{make_float2(x, y)};
+    float4 v;   // dx, dy, d^2, index (int bits)
+    __device__ __forceinline__ int j() const { return __float_as_int(v.w); }
+    __device__ __forceinline__ static QEntry make(float dx, float dy, float d2, int j) {
+        return QEntry{make_float4(dx, dy, d2, __int_as_float(j))};
     }
 };
 template <>
@@ -241,6 +242,40 @@ static NoAllocDevice *noalloc_device(int *status) {
     return &devs[dev];
 }
 
+// Double-float re-decision of one deferred pair (xj, yj, rj: the neighbour's position and
+// radius) and its rasterisation; returns whether a re-decided boundary lies within 1e-9 rad
+// of the pair's edge angle.
+template <bool TORUS, bool HETERO>
+__device__ __forceinline__ bool resolve_and_raster(const FocalDev &f, float xj, float yj, float rj,
+                                                   uint32_t *vb, const StepArgs &a) {
+    float dx, dy;
+    pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
+    const PairEst de = estimate_pair<HETERO>(f, dx, dy, rj, HETERO ? rcp_approx(rj) : f.invr,
+                                             a.g);
+    dfl ex, ey;
+    exact_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, ex, ey);
+    const int3 th = resolve_pair(f.cd, f.sd, ex, ey, rj, resolve_grid(a.g), de.unc_t, de.unc_h,
+                                 de.u, de.ps2, de.t, de.h);
+    const int ds = th.x - th.y, dn = th.x + th.y;
+    if (projection_visible(a.g, ds, dn)) raster_fast(vb, a.g.rv, ds, dn);
+    return th.z != 0;
+}
+
+// The neighbour a deferred queue entry stands for: position and radius.
+template <bool HETERO>
+__device__ __forceinline__ void deferred_neighbour(const QEntry<HETERO> &d, const StepArgs &a,
+                                                   float &xj, float &yj, float &rj) {
+    if constexpr (HETERO) {
+        xj = d.x();
+        yj = d.y();
+        rj = d.r(a.radius0);
+    } else {
+        xj = __ldg(a.x + d.j());
+        yj = __ldg(a.y + d.j());
+        rj = a.radius0;
+    }
+}
+
 // Heavy decision + rasterisation of up to 32 queued candidates (lane < cnt holds one).
 template <bool TORUS, bool HETERO, bool FULL = false>
 __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEntry<HETERO> *q,
@@ -249,36 +284,41 @@ __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEnt
                                                    unsigned *cnt_resolved, unsigned *cnt_near) {
     const int lane = threadIdx.x & 31;
     const bool have = FULL || lane < cnt;   // FULL: a batch of 32, every lane has a candidate
-    QEntry<HETERO> e = (FULL || have) ? q[lane] : QEntry<HETERO>::make(f.x, f.y, f.r);
-    const float xj = e.x(), yj = e.y(), rj = e.r(a.radius0);
-    float dx, dy;
-    pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
-    const PairEst est = estimate_pair<HETERO>(f, dx, dy, rj, HETERO ? rcp_approx(rj) : f.invr,
-                                              a.g);
-    const bool unc = have && (est.unc_t || est.unc_h);
+    bool unc;
+    int s, en;
+    QEntry<HETERO> e;
+    if constexpr (!HETERO) {
+        // from the queued offset; overlapping discs and guard-band decisions are deferred
+        e = (FULL || have) ? q[lane] : QEntry<false>::make(1.f, 0.f, 1.f, 0);
+        const FastEst est = estimate_fast(f, e.v.x, e.v.y, e.v.z, f.r, f.r * f.r, a.g);
+        unc = have && est.unc;
+        s = est.t - est.h;
+        en = est.t + est.h;
+        if (have && !est.unc && (a.g.full_fov || projection_visible(a.g, s, en)))
+            raster_fast(vb, a.g.rv, s, en);
+    } else {
+        e = (FULL || have) ? q[lane] : QEntry<true>::make(f.x, f.y, f.r);
+        const float xj = e.x(), yj = e.y(), rj = e.r(a.radius0);
+        float dx, dy;
+        pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
+        const PairEst est = estimate_pair<HETERO>(f, dx, dy, rj, rcp_approx(rj), a.g);
+        unc = have && (est.unc_t || est.unc_h);
+        s = est.t - est.h;
+        en = est.t + est.h;
+        if (have && !unc && projection_visible(a.g, s, en)) raster_fast(vb, a.g.rv, s, en);
+    }
     const unsigned um = __ballot_sync(ABM_FULL_MASK, unc);
     if (um) {  // defer the uncertain ones to the double-float queue
         if (unc) q2[q2n + __popc(um & ((1u << lane) - 1u))] = e;
         q2n += __popc(um);
     }
-    const int s = est.t - est.h, en = est.t + est.h;
-    if (have && !unc && projection_visible(a.g, s, en)) raster_fast(vb, a.g.rv, s, en);
     __syncwarp();
     if (q2n >= 32) {   // drain 32 deferred pairs (warp-uniform)
         q2n -= 32;
-        const QEntry<HETERO> d = q2[q2n + lane];
-        const float dxj = d.x(), dyj = d.y(), drj = d.r(a.radius0);
-        float ddx, ddy;
-        pair_offset<TORUS, HETERO>(f, dxj, dyj, drj, a.W, a.H, ddx, ddy);
-        const PairEst de = estimate_pair<HETERO>(f, ddx, ddy, drj,
-                                                 HETERO ? rcp_approx(drj) : f.invr, a.g);
-        dfl ex, ey;
-        exact_offset<TORUS, HETERO>(f, dxj, dyj, drj, a.W, a.H, ex, ey);
-        const int3 th = resolve_pair(f.cd, f.sd, ex, ey, drj, resolve_grid(a.g), de.unc_t,
-                                     de.unc_h, de.u, de.ps2, de.t, de.h);
-        const int ds = th.x - th.y, dn = th.x + th.y;
-        if (projection_visible(a.g, ds, dn)) raster_fast(vb, a.g.rv, ds, dn);
-        const unsigned nm = __ballot_sync(ABM_FULL_MASK, th.z != 0);
+        float xj, yj, rj;
+        deferred_neighbour<HETERO>(q2[q2n + lane], a, xj, yj, rj);
+        const bool near = resolve_and_raster<TORUS, HETERO>(f, xj, yj, rj, vb, a);
+        const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
         if (lane == 0) {
             atomicAdd(cnt_resolved, 32u);
             if (nm) atomicAdd(cnt_near, (unsigned)__popc(nm));
@@ -296,19 +336,9 @@ __device__ __forceinline__ void drain_deferred(const FocalDev &f, const QEntry<H
     if (q2n == 0) return;
     bool near = false;
     if (lane < q2n) {
-        const QEntry<HETERO> d = q2[lane];
-        const float xj = d.x(), yj = d.y(), rj = d.r(a.radius0);
-        float dx, dy;
-        pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
-        const PairEst de = estimate_pair<HETERO>(f, dx, dy, rj,
-                                                 HETERO ? rcp_approx(rj) : f.invr, a.g);
-        dfl ex, ey;
-        exact_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, ex, ey);
-        const int3 th = resolve_pair(f.cd, f.sd, ex, ey, rj, resolve_grid(a.g), de.unc_t,
-                                     de.unc_h, de.u, de.ps2, de.t, de.h);
-        const int ds = th.x - th.y, dn = th.x + th.y;
-        if (projection_visible(a.g, ds, dn)) raster_fast(vb, a.g.rv, ds, dn);
-        near = th.z != 0;
+        float xj, yj, rj;
+        deferred_neighbour<HETERO>(q2[lane], a, xj, yj, rj);
+        near = resolve_and_raster<TORUS, HETERO>(f, xj, yj, rj, vb, a);
     }
     const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
     if (lane == 0) {
@@ -332,36 +362,37 @@ __device__ __forceinline__ FocalDev load_focal(const StepArgs &a, int i) {
     return f;
 }
 
-// Phase A for one lane's neighbour: the exact-zero / cull test of vf_supcalc.py:57-58 and
-// h = 0 (projections narrower than 2 pixels never fill anything).
+// Phase A for one lane's neighbour j: the exact-zero / cull test of vf_supcalc.py:57-58 and
+// h = 0 (projections narrower than 2 pixels never fill anything); the live candidate is
+// appended to the warp queue, and phase B runs on every full batch of 32.
 template <bool TORUS, bool HETERO>
-__device__ __forceinline__ bool candidate_live(const FocalDev &f, float xj, float yj, float rj,
-                                               bool valid, float cull_r2, const StepArgs &a) {
+__device__ __forceinline__ void phase_a(const FocalDev &f, float xj, float yj, float rj, int j,
+                                        bool valid, float cull_r2, QEntry<HETERO> *q, int &qn,
+                                        QEntry<HETERO> *q2, int &q2n, uint32_t *vb,
+                                        const StepArgs &a, unsigned *counters) {
+    const int lane = threadIdx.x & 31;
     float dx, dy;
     pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
     const float d2 = fmaf(dx, dx, dy * dy);
-    if (HETERO) {
+    bool live;
+    if constexpr (HETERO) {
         const bool same = (xj == f.x) && (yj == f.y);
-        return valid && !same && d2 <= rj * rj * a.g.cull;
+        live = valid && !same && d2 <= rj * rj * a.g.cull;
+    } else {
+        live = valid && d2 > 0.f && d2 <= cull_r2;   // equal radii: same position <=> zero offset
     }
-    return valid && d2 > 0.f && d2 <= cull_r2;   // equal radii: same position <=> zero offset
-}
-
-// Append the lane's live candidate to the warp queue; run phase B on every full batch of 32.
-template <bool TORUS, bool HETERO>
-__device__ __forceinline__ void enqueue_candidate(const FocalDev &f, bool live, float xj, float yj,
-                                                  float rj, QEntry<HETERO> *q, int &qn,
-                                                  QEntry<HETERO> *q2, int &q2n, uint32_t *vb,
-                                                  const StepArgs &a, unsigned *counters) {
-    const int lane = threadIdx.x & 31;
     const unsigned lm = __ballot_sync(ABM_FULL_MASK, live);
-    if (live) q[qn + __popc(lm & ((1u << lane) - 1u))] = QEntry<HETERO>::make(xj, yj, rj);
+    if (live) {
+        QEntry<HETERO> *slot = q + qn + __popc(lm & ((1u << lane) - 1u));
+        if constexpr (HETERO) *slot = QEntry<true>::make(xj, yj, rj);
+        else *slot = QEntry<false>::make(dx, dy, d2, j);
+    }
     qn += __popc(lm);
     __syncwarp();
     if (qn >= 32) {   // warp-uniform
         qn -= 32;
         process_candidates<TORUS, HETERO, true>(f, q + qn, 32, q2, q2n, vb, a, &counters[0],
-                                          &counters[1]);
+                                                &counters[1]);
     }
 }
 
@@ -394,7 +425,8 @@ __device__ __forceinline__ void flush_counters(const StepArgs &a, const unsigned
 // ---------------------------------------------------------------------------- l1 form
 // One block = one focal agent, WPA warps share its bitmask and split its neighbours.
 static size_t l1_smem_bytes(int wpa, int words, bool hetero) {
-    const size_t qe = hetero ? 16 : 8;
+    const size_t qe = sizeof(QEntry<false>);
+    (void)hetero;
     size_t b = (size_t)words * sizeof(uint32_t);
     b = (b + 15) & ~size_t(15);
     b += (size_t)wpa * (kQueue + kQueue2) * qe;
@@ -447,8 +479,8 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
             yn = __ldg(a.y + jn);
             if (HETERO) rn = __ldg(a.radius + jn);
         }
-        const bool live = candidate_live<TORUS, HETERO>(f, xj, yj, rj, valid, cull_r2, a);
-        enqueue_candidate<TORUS, HETERO>(f, live, xj, yj, rj, q, qn, q2, q2n, vb, a, counters);
+        phase_a<TORUS, HETERO>(f, xj, yj, rj, jb + lane, valid, cull_r2, q, qn, q2, q2n, vb, a,
+                               counters);
     }
     if (qn > 0) process_candidates<TORUS, HETERO>(f, q, qn, q2, q2n, vb, a, &counters[0],
                                                   &counters[1]);
@@ -474,7 +506,7 @@ static int tile_buffers(int n, int tile) { return n > tile ? 2 : 1; }
 
 static size_t tiled_smem_bytes(int warps, int tile, int words, bool hetero, int nbuf) {
     const int nf = hetero ? 3 : 2;
-    const size_t qe = hetero ? 16 : 8;
+    const size_t qe = sizeof(QEntry<false>);
     size_t b = 16 + (size_t)nbuf * nf * tile * sizeof(float);
     b += (size_t)warps * words * sizeof(uint32_t);
     b = (b + 15) & ~size_t(15);
@@ -582,9 +614,8 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
                     yj = a.y[base + jj];
                     if (HETERO) rj = a.radius[base + jj];
                 }
-                const bool live = candidate_live<TORUS, HETERO>(f, xj, yj, rj, valid, cull_r2, a);
-                enqueue_candidate<TORUS, HETERO>(f, live, xj, yj, rj, q, qn, q2, q2n, vb, a,
-                                                 counters);
+                phase_a<TORUS, HETERO>(f, xj, yj, rj, base + jj, valid, cull_r2, q, qn, q2, q2n,
+                                       vb, a, counters);
             }
         }
         __syncthreads();

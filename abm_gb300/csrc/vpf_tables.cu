@@ -165,6 +165,7 @@ int build_grid_host(int rv, double fov0, double fov1, GridHostTables &t) {
     g.f0 = find_nearest(phis, fov0);
     g.f1 = find_nearest(phis, fov1);
     g.kmax = (rv + 3) / 4;
+    g.full_fov = (g.f0 == 0 && g.f1 == rv - 1 && rv >= 3) ? 1 : 0;
     const double inv_delta = (double)(rv - 1) / (2 * kPi);
     g.inv_delta = (float)inv_delta;
     g.half_rm1 = (float)(0.5 * (rv - 1));
