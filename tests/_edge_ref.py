@@ -130,3 +130,46 @@ def loss(x, y, th, target, R=0.0):
     pol = torch.sqrt(torch.cos(th).sum() ** 2 + torch.sin(th).sum() ** 2) / n
     mx, my = (x + R).mean(), (y + R).mean()
     return 1.0 - pol + ((mx - target[0]) ** 2 + (my - target[1]) ** 2) / 2.0
+
+
+def event_margins(x, y, th, R, bounds, v=None, p=None, dt=0.1):
+    """Per focal agent, the distance (radians) of its arc structure from the nearest event of
+    the edge form -- an arc start decision (lower end vs the running maximum of the upper ends),
+    the seam fold (lower end + 2 pi vs the last upper end), the wrap of a lower end at -pi or
+    of a bearing at +-pi -- and, when the update's inputs v, p are given, the distance (pixels)
+    of its new centre from a wall.  A gradient is a derivative of the step only away from these
+    discontinuities."""
+    n = x.shape[0]
+    dx = x[None, :] - x[:, None]
+    dy = y[None, :] - y[:, None]
+    eye = torch.eye(n, dtype=torch.bool, device=x.device)
+    valid = ~eye & ((dx != 0) | (dy != 0))
+    dxs = torch.where(valid, dx, torch.ones_like(dx))
+    dys = torch.where(valid, dy, torch.zeros_like(dy))
+    b = torch.atan2(-dys, dxs) - th[:, None]
+    b = b - TWO_PI * torch.round(b / TWO_PI)
+    a = torch.atan(R / torch.sqrt(dxs * dxs + dys * dys))
+    lo = b - a
+    m_wrap = torch.where(valid, torch.minimum((lo + math.pi).abs(), (b.abs() - math.pi).abs()),
+                         torch.full_like(lo, BIG))
+    lo = torch.where(lo < -math.pi, lo + TWO_PI, lo)
+    up = lo + 2 * a
+    lo = torch.where(valid, lo, torch.full_like(lo, BIG))
+    up = torch.where(valid, up, torch.full_like(up, -BIG))
+    lo_s, order = torch.sort(lo, dim=1)
+    up_s = torch.gather(up, 1, order)
+    pm = torch.cummax(up_s, dim=1).values
+    vmask = lo_s < BIG / 2
+    gap = (lo_s[:, 1:] - pm[:, :-1]).abs()
+    gap = torch.where(vmask[:, 1:], gap, torch.full_like(gap, BIG))
+    ulast = pm.gather(1, (vmask.sum(1, keepdim=True) - 1).clamp(min=0))
+    fold = torch.where(vmask, (lo_s + TWO_PI - ulast).abs(), torch.full_like(lo_s, BIG))
+    m = torch.minimum(torch.minimum(gap.min(1).values, fold.min(1).values), m_wrap.min(1).values)
+    out = {"arc": m}
+    if v is not None and p is not None:
+        x1, y1, _, _ = edge_step(x, y, th, v, p, R, dt, bounds)
+        bx0, bx1, by0, by1 = bounds
+        cx, cy = x1 + R, y1 + R
+        out["wall"] = torch.stack([(cx - bx0).abs(), (cx - bx1).abs(), (cy - by0).abs(),
+                                   (cy - by1).abs()], 1).min(1).values
+    return out
