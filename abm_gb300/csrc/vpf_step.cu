@@ -42,6 +42,9 @@ struct StepArgs {
     // into vbits (n x words, zero between steps); NULL for the one-block-per-agent form
     uint32_t *vbits;
     int chunk_shift, chunk_len;
+    // x and y 8-byte aligned: the l1 form reads two adjacent neighbours per lane (walls, equal
+    // radii)
+    int pair_loads;
     // batched sweeps: agent i sees the agents [seg_begin[i], seg_end[i]) of its instance;
     // block b works on agent order[b] (largest instances first); all NULL for one swarm
     const int *seg_begin, *seg_end, *order;
@@ -167,7 +170,7 @@ static void *device_view(const void *host) {
 // Per-warp work queues of the step kernel: candidate neighbours that survived the cull (their
 // positions, so the queue outlives the tile) and pairs whose FP32 decision needs the
 // double-float re-decision.
-constexpr int kQueue = 64;
+constexpr int kQueue = 96;    // < 32 left + up to 64 appended per phase-A round
 constexpr int kQueue2 = 64;
 
 // A queued candidate.  Equal radii: the pair's FP32 centre offset, d^2 and the neighbour's
@@ -462,15 +465,60 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
     if (WPA > 1) __syncthreads(); else __syncwarp();
 
     int qn = 0, q2n = 0;
+    bool paired = false;
+    if constexpr (!TORUS && !HETERO) {
+      paired = a.pair_loads != 0;
+      if (paired) {
+        // two adjacent neighbours per lane, 64 per warp and round: one 8-byte load per
+        // coordinate, packed FP32x2 offsets and distances (the same roundings as one by one)
+        constexpr int kStep2 = 64 * WPA;
+        const int jb0 = (j0 & ~1) + warp * 64;   // even, so the pairs are 8-byte aligned
+        float2 xn2 = make_float2(f.x, f.x), yn2 = make_float2(f.y, f.y);
+        auto load2 = [&](int jj, float2 &xv, float2 &yv) {
+            if (jj + 1 < n) {
+                xv = __ldg(reinterpret_cast<const float2 *>(a.x + jj));
+                yv = __ldg(reinterpret_cast<const float2 *>(a.y + jj));
+            } else if (jj < n) {
+                xv = make_float2(__ldg(a.x + jj), f.x);
+                yv = make_float2(__ldg(a.y + jj), f.y);
+            }
+        };
+        load2(jb0 + 2 * lane, xn2, yn2);
+        const unsigned lt = (1u << lane) - 1u;
+        for (int jb = jb0; jb < n; jb += kStep2) {
+            const float2 xv = xn2, yv = yn2;
+            const int jj = jb + 2 * lane;
+            load2(jb + kStep2 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
+            const float2 dx = __fadd2_rn(xv, make_float2(-f.x, -f.x));
+            const float2 dy = __fadd2_rn(yv, make_float2(-f.y, -f.y));
+            const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+            const bool live0 = jj >= j0 && jj < n && d2.x > 0.f && d2.x <= cull_r2;
+            const bool live1 = jj + 1 >= j0 && jj + 1 < n && d2.y > 0.f && d2.y <= cull_r2;
+            const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
+            const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
+            const int c0 = __popc(lm0);
+            if (live0) q[qn + __popc(lm0 & lt)] = QEntry<HETERO>::make(dx.x, dy.x, d2.x, jj);
+            if (live1)
+                q[qn + c0 + __popc(lm1 & lt)] = QEntry<HETERO>::make(dx.y, dy.y, d2.y, jj + 1);
+            qn += c0 + __popc(lm1);
+            __syncwarp();
+            while (qn >= 32) {   // warp-uniform; at most two batches
+                qn -= 32;
+                process_candidates<TORUS, HETERO, true>(f, q + qn, 32, q2, q2n, vb, a,
+                                                        &counters[0], &counters[1]);
+            }
+        }
+      }
+    }
     constexpr int kStep = 32 * WPA;
     int j = j0 + warp * 32 + lane;
     float xn = f.x, yn = f.y, rn = f.r;
-    if (j < n) {
+    if (!paired && j < n) {
         xn = __ldg(a.x + j);
         yn = __ldg(a.y + j);
         if (HETERO) rn = __ldg(a.radius + j);
     }
-    for (int jb = j0 + warp * 32; jb < n; jb += kStep) {
+    for (int jb = j0 + warp * 32; !paired && jb < n; jb += kStep) {
         const float xj = xn, yj = yn, rj = rn;
         const bool valid = jb + lane < n;
         const int jn = jb + kStep + lane;   // prefetch the next chunk through L1
@@ -1279,6 +1327,7 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     a.sctab = sctab;
     a.sums = ws.sums;
     a.vbits = seg_begin ? nullptr : ws.vbits;
+    a.pair_loads = ((uintptr_t)in->x % 8 == 0 && (uintptr_t)in->y % 8 == 0) ? 1 : 0;
     a.g = *g;
     a.seg_begin = seg_begin;
     a.seg_end = seg_end;
