@@ -405,6 +405,18 @@ __device__ __forceinline__ bool projection_visible(const GridDev &g, int s, int 
     return (unsigned)(s - g.f0 - 1) < span || (unsigned)(e - g.f0 - 1) < span;
 }
 
+// OR a run [s, s + len) of at most 32 pixels (0 <= s, s + len <= Rv) into the bitmask: at most
+// two words, two predicated shared atomics.
+__device__ __forceinline__ void raster_short(uint32_t *vb, int s, unsigned len) {
+    // len ones (0xffffffff >> (32 - len), none for len = 0) shifted to bit s & 31
+    const uint32_t m = __funnelshift_rc(ABM_FULL_MASK, 0u, 32u - len);
+    const int w0 = s >> 5, sh = s & 31;
+    const uint32_t lo = m << sh;
+    const uint32_t hi = __funnelshift_l(m, 0u, sh);
+    if (lo) atomicOr(&vb[w0], lo);
+    if (hi) atomicOr(&vb[w0 + 1], hi);
+}
+
 // OR a visible projection [s, e) into the bitmask; the common case (no wrap, at most 32
 // pixels) is two predicated shared atomics, the rest goes through raster_projection.
 __device__ __forceinline__ void raster_fast(uint32_t *vb, int rv, int s, int e) {
@@ -698,7 +710,7 @@ struct UpdateOut {
     dfl terms[6];   // dvel, dpsi, alpha_blob, alpha_edge, beta_blob, beta_edge
 };
 
-static __device__ __noinline__ UpdateOut update_agent_df(const UpdateDf &p, const float4 *sctab,
+__device__ __forceinline__ UpdateOut update_agent_df(const UpdateDf &p, const float4 *sctab,
                                                   float xf, float yf, float thf, float vf,
                                                   float Rf, long long bc, long long bs,
                                                   long long ec, long long es, dfl alp0,

@@ -172,6 +172,7 @@ static void *device_view(const void *host) {
 // double-float re-decision.
 constexpr int kQueue = 96;    // < 32 left + up to 64 appended per phase-A round
 constexpr int kQueue2 = 64;
+constexpr int kQueueW = 64;   // runs longer than 32 pixels or wrapping at the seam (s, e)
 
 // A queued candidate.  Equal radii: the pair's FP32 centre offset, d^2 and the neighbour's
 // index (so phase B starts from the offset, and the rare double-float re-decision reloads the
@@ -283,8 +284,9 @@ __device__ __forceinline__ void deferred_neighbour(const QEntry<HETERO> &d, cons
 template <bool TORUS, bool HETERO, bool FULL = false>
 __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEntry<HETERO> *q,
                                                    int cnt, QEntry<HETERO> *q2, int &q2n,
-                                                   uint32_t *vb, const StepArgs &a,
-                                                   unsigned *cnt_resolved, unsigned *cnt_near) {
+                                                   int2 *wq, int &wqn, uint32_t *vb,
+                                                   const StepArgs &a, unsigned *cnt_resolved,
+                                                   unsigned *cnt_near) {
     const int lane = threadIdx.x & 31;
     const bool have = FULL || lane < cnt;   // FULL: a batch of 32, every lane has a candidate
     bool unc;
@@ -297,8 +299,24 @@ __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEnt
         unc = have && est.unc;
         s = est.t - est.h;
         en = est.t + est.h;
-        if (have && !est.unc && (a.g.full_fov || projection_visible(a.g, s, en)))
-            raster_fast(vb, a.g.rv, s, en);
+        const bool vis = have && !est.unc && (a.g.full_fov || projection_visible(a.g, s, en));
+        const unsigned len = (unsigned)(en - s);
+        const bool short_run = s >= 0 && en < a.g.rv && len <= 32u;
+        if (vis && short_run) raster_short(vb, s, len);
+        // long and wrapping runs wait in the warp's run queue, drained 32 at a time, so that
+        // the rare lane that needs the general fill does not hold up the other 31
+        const unsigned wm = __ballot_sync(ABM_FULL_MASK, vis && !short_run);
+        if (wm) {
+            if (vis && !short_run) wq[wqn + __popc(wm & ((1u << lane) - 1u))] = make_int2(s, en);
+            wqn += __popc(wm);
+            __syncwarp();
+            if (wqn >= 32) {
+                wqn -= 32;
+                const int2 r = wq[wqn + lane];
+                raster_projection(vb, a.g.rv, r.x, r.y);
+                __syncwarp();
+            }
+        }
     } else {
         e = (FULL || have) ? q[lane] : QEntry<true>::make(f.x, f.y, f.r);
         const float xj = e.x(), yj = e.y(), rj = e.r(a.radius0);
@@ -328,6 +346,17 @@ __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEnt
         }
         __syncwarp();
     }
+}
+
+// The last (< 32) queued long or wrapping runs.
+__device__ __forceinline__ void flush_runs(const int2 *wq, int wqn, uint32_t *vb, int rv) {
+    const int lane = threadIdx.x & 31;
+    if (wqn == 0) return;
+    if (lane < wqn) {
+        const int2 r = wq[lane];
+        raster_projection(vb, rv, r.x, r.y);
+    }
+    __syncwarp();
 }
 
 // Double-float resolution of the last (< 32) deferred pairs.
@@ -371,8 +400,8 @@ __device__ __forceinline__ FocalDev load_focal(const StepArgs &a, int i) {
 template <bool TORUS, bool HETERO>
 __device__ __forceinline__ void phase_a(const FocalDev &f, float xj, float yj, float rj, int j,
                                         bool valid, float cull_r2, QEntry<HETERO> *q, int &qn,
-                                        QEntry<HETERO> *q2, int &q2n, uint32_t *vb,
-                                        const StepArgs &a, unsigned *counters) {
+                                        QEntry<HETERO> *q2, int &q2n, int2 *wq, int &wqn,
+                                        uint32_t *vb, const StepArgs &a, unsigned *counters) {
     const int lane = threadIdx.x & 31;
     float dx, dy;
     pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
@@ -394,8 +423,8 @@ __device__ __forceinline__ void phase_a(const FocalDev &f, float xj, float yj, f
     __syncwarp();
     if (qn >= 32) {   // warp-uniform
         qn -= 32;
-        process_candidates<TORUS, HETERO, true>(f, q + qn, 32, q2, q2n, vb, a, &counters[0],
-                                                &counters[1]);
+        process_candidates<TORUS, HETERO, true>(f, q + qn, 32, q2, q2n, wq, wqn, vb, a,
+                                                &counters[0], &counters[1]);
     }
 }
 
@@ -432,7 +461,7 @@ static size_t l1_smem_bytes(int wpa, int words, bool hetero) {
     (void)hetero;
     size_t b = (size_t)words * sizeof(uint32_t);
     b = (b + 15) & ~size_t(15);
-    b += (size_t)wpa * (kQueue + kQueue2) * qe;
+    b += (size_t)wpa * ((kQueue + kQueue2) * qe + kQueueW * sizeof(int2));
     return b + 16;
 }
 
@@ -455,6 +484,8 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
     QEntry<HETERO> *q = reinterpret_cast<QEntry<HETERO> *>(smem + off) + warp * (kQueue + kQueue2);
     QEntry<HETERO> *q2 = q + kQueue;
     off += (size_t)WPA * (kQueue + kQueue2) * sizeof(QEntry<HETERO>);
+    int2 *wq = reinterpret_cast<int2 *>(smem + off) + warp * kQueueW;
+    off += (size_t)WPA * kQueueW * sizeof(int2);
     unsigned *counters = reinterpret_cast<unsigned *>(smem + off);
 
     for (int w = threadIdx.x; w < words; w += 32 * WPA) vb[w] = 0u;
@@ -464,7 +495,7 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
     const float cull_r2 = f.r * f.r * a.g.cull;
     if (WPA > 1) __syncthreads(); else __syncwarp();
 
-    int qn = 0, q2n = 0;
+    int qn = 0, q2n = 0, wqn = 0;
     bool paired = false;
     if constexpr (!TORUS && !HETERO) {
       paired = a.pair_loads != 0;
@@ -504,8 +535,8 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
             __syncwarp();
             while (qn >= 32) {   // warp-uniform; at most two batches
                 qn -= 32;
-                process_candidates<TORUS, HETERO, true>(f, q + qn, 32, q2, q2n, vb, a,
-                                                        &counters[0], &counters[1]);
+                process_candidates<TORUS, HETERO, true>(f, q + qn, 32, q2, q2n, wq, wqn, vb,
+                                                        a, &counters[0], &counters[1]);
             }
         }
       }
@@ -527,11 +558,12 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
             yn = __ldg(a.y + jn);
             if (HETERO) rn = __ldg(a.radius + jn);
         }
-        phase_a<TORUS, HETERO>(f, xj, yj, rj, jb + lane, valid, cull_r2, q, qn, q2, q2n, vb, a,
-                               counters);
+        phase_a<TORUS, HETERO>(f, xj, yj, rj, jb + lane, valid, cull_r2, q, qn, q2, q2n, wq,
+                               wqn, vb, a, counters);
     }
-    if (qn > 0) process_candidates<TORUS, HETERO>(f, q, qn, q2, q2n, vb, a, &counters[0],
-                                                  &counters[1]);
+    if (qn > 0) process_candidates<TORUS, HETERO>(f, q, qn, q2, q2n, wq, wqn, vb, a,
+                                                  &counters[0], &counters[1]);
+    flush_runs(wq, wqn, vb, a.g.rv);
     drain_deferred<TORUS, HETERO>(f, q2, q2n, vb, a, &counters[0], &counters[1]);
     if (WPA > 1) __syncthreads(); else __syncwarp();
     if (split) {   // partial bitmask into the agent's global one; integrals in the finish kernel
@@ -558,7 +590,7 @@ static size_t tiled_smem_bytes(int warps, int tile, int words, bool hetero, int 
     size_t b = 16 + (size_t)nbuf * nf * tile * sizeof(float);
     b += (size_t)warps * words * sizeof(uint32_t);
     b = (b + 15) & ~size_t(15);
-    b += (size_t)warps * (kQueue + kQueue2) * qe;
+    b += (size_t)warps * ((kQueue + kQueue2) * qe + kQueueW * sizeof(int2));
     b += 16;  // block counters
     return b;
 }
@@ -579,6 +611,8 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
     QEntry<HETERO> *q = reinterpret_cast<QEntry<HETERO> *>(smem + off) + warp * (kQueue + kQueue2);
     QEntry<HETERO> *q2 = q + kQueue;
     off += (size_t)nw * (kQueue + kQueue2) * sizeof(QEntry<HETERO>);
+    int2 *wq = reinterpret_cast<int2 *>(smem + off) + warp * kQueueW;
+    off += (size_t)nw * kQueueW * sizeof(int2);
     unsigned *counters = reinterpret_cast<unsigned *>(smem + off);
 
     const int i = blockIdx.x * nw + warp;
@@ -613,7 +647,7 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
     };
     if (TMA && tid == 0) issue(0);
 
-    int qn = 0, q2n = 0;
+    int qn = 0, q2n = 0, wqn = 0;
     for (int k = 0; k < ntiles; ++k) {
         const int base = k * tile;
         const int tn = min(tile, n - base);
@@ -663,14 +697,15 @@ __global__ void __launch_bounds__(1024) vpf_pairs_tiled_kernel(const StepArgs a)
                     if (HETERO) rj = a.radius[base + jj];
                 }
                 phase_a<TORUS, HETERO>(f, xj, yj, rj, base + jj, valid, cull_r2, q, qn, q2, q2n,
-                                       vb, a, counters);
+                                       wq, wqn, vb, a, counters);
             }
         }
         __syncthreads();
     }
     if (active) {
-        if (qn > 0) process_candidates<TORUS, HETERO>(f, q, qn, q2, q2n, vb, a, &counters[0],
-                                                      &counters[1]);
+        if (qn > 0) process_candidates<TORUS, HETERO>(f, q, qn, q2, q2n, wq, wqn, vb, a,
+                                                      &counters[0], &counters[1]);
+        flush_runs(wq, wqn, vb, a.g.rv);
         drain_deferred<TORUS, HETERO>(f, q2, q2n, vb, a, &counters[0], &counters[1]);
         __syncwarp();
         finish_agent(a, i, vb, reinterpret_cast<uint32_t *>(q), kListCap<HETERO>);
@@ -738,6 +773,10 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
     extern __shared__ __align__(16) unsigned char fsmem[];
     __shared__ longlong2 sums[kFinishWarps][2];
     __shared__ FinishInputs uin[kFinishWarps];
+    // the double-float sincos table of the update, staged while the pair kernel drains, so
+    // that the lookup of the new heading's cos/sin is a shared-memory load
+    __shared__ float4 s_sincos[kSinCosTab];
+    for (int t = threadIdx.x; t < kSinCosTab; t += blockDim.x) s_sincos[t] = __ldg(a.sctab + t);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, words = a.g.words;
     const int k = blockIdx.x * kFinishWarps + warp;
     const int ku = blockIdx.x * kFinishWarps + lane;
@@ -798,7 +837,7 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
     const dfl alp0 = a.alp0 ? dfl{in.alp0, 0.f} : a.ud.alp0;
     const dfl bet0 = a.bet0 ? dfl{in.bet0, 0.f} : a.ud.bet0;
     const dfl v0 = a.v0 ? dfl{in.v0, 0.f} : a.ud.v0;
-    const UpdateOut o = update_agent_df(a.ud, a.sctab, in.x, in.y, in.th, in.v, in.R, s0.x,
+    const UpdateOut o = update_agent_df(a.ud, s_sincos, in.x, in.y, in.th, in.v, in.R, s0.x,
                                         s0.y, s1.x, s1.y, alp0, bet0, v0);
     store_update(a, ku, o);
 }
