@@ -52,7 +52,7 @@ struct StepArgs {
 
 static int g_warps = 8;    // tiled form: focal warps per block
 static int g_tile = 8192;  // tiled form: neighbour tile length
-static int g_mode = 0;     // 0 auto, 1 l1, 2 tiled
+static int g_mode = 0;     // 0 auto, 1 l1, 2 tiled, 3 group
 static int g_wpa = 1;      // l1 form: warps per focal agent
 static int g_split = 0;    // l1 form: neighbour chunks per agent (0 auto, else a power of two)
 static std::mutex g_cfg_mu;
@@ -579,6 +579,189 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
     }
 }
 
+// ---------------------------------------------------------------------------- group form
+// One warp serves kGroup consecutive focal agents of a single swarm (walls, equal radii):
+// phase A reads each neighbour once for the whole group, and the candidate queue mixes the
+// group's agents -- each entry carries the agent's slot in the group in the top byte of its
+// neighbour index -- so the batches of phase B stay full, and the per-block costs (focal
+// set-up, the last partial batch, the double-float drain, the long-run flush, the epilogue)
+// are paid once per kGroup agents.  With a.vbits set the neighbours are split into chunks
+// exactly as in the l1 form and the group's partial bitmasks are OR-ed into the workspace.
+constexpr int kGroup = 4;
+constexpr int kGroupTagShift = 24;   // neighbour indices below 2^24
+
+static size_t group_smem_bytes(int words) {
+    size_t b = ((size_t)kGroup * words * sizeof(uint32_t) + 15) & ~size_t(15);
+    b += ((size_t)kGroup * sizeof(FocalDev) + 15) & ~size_t(15);
+    b += (size_t)(kQueue + kQueue2) * sizeof(QEntry<false>) + kQueueW * sizeof(int2);
+    return b + 16;
+}
+
+// Phase B of up to 32 queued (agent slot, neighbour) candidates (lane < cnt holds one).
+template <bool FULL>
+__device__ __forceinline__ void group_batch(const FocalDev *fd, const QEntry<false> *q, int cnt,
+                                            QEntry<false> *q2, int &q2n, int2 *wq, int &wqn,
+                                            uint32_t *vball, const StepArgs &a,
+                                            unsigned *counters) {
+    const int lane = threadIdx.x & 31;
+    const int words = a.g.words;
+    const bool have = FULL || lane < cnt;
+    const QEntry<false> e = (FULL || have) ? q[lane] : QEntry<false>::make(1.f, 0.f, 1.f, 0);
+    const int g = (int)((unsigned)e.j() >> kGroupTagShift);
+    const FastEst est = estimate_fast(fd[g], e.v.x, e.v.y, e.v.z, a.radius0,
+                                      a.radius0 * a.radius0, a.g);
+    const bool unc = have && est.unc;
+    const int s = est.t - est.h, en = est.t + est.h;
+    const bool vis = have && !est.unc && (a.g.full_fov || projection_visible(a.g, s, en));
+    const unsigned len = (unsigned)(en - s);
+    const bool short_run = s >= 0 && en < a.g.rv && len <= 32u;
+    if (vis && short_run) raster_short(vball + g * words, s, len);
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned wm = __ballot_sync(ABM_FULL_MASK, vis && !short_run);
+    if (wm) {   // long and wrapping runs wait in the run queue (slot in the top byte of e)
+        if (vis && !short_run) wq[wqn + __popc(wm & lt)] = make_int2(s, en | (g << kGroupTagShift));
+        wqn += __popc(wm);
+        __syncwarp();
+        if (wqn >= 32) {
+            wqn -= 32;
+            const int2 r = wq[wqn + lane];
+            raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
+                              r.y & ((1 << kGroupTagShift) - 1));
+            __syncwarp();
+        }
+    }
+    const unsigned um = __ballot_sync(ABM_FULL_MASK, unc);
+    if (um) {   // defer the uncertain ones to the double-float queue
+        if (unc) q2[q2n + __popc(um & lt)] = e;
+        q2n += __popc(um);
+    }
+    __syncwarp();
+    if (q2n >= 32) {   // drain 32 deferred pairs (warp-uniform)
+        q2n -= 32;
+        const int tag = q2[q2n + lane].j();
+        const int dg = (int)((unsigned)tag >> kGroupTagShift);
+        const int j = tag & ((1 << kGroupTagShift) - 1);
+        const bool near = resolve_and_raster<false, false>(fd[dg], __ldg(a.x + j), __ldg(a.y + j),
+                                                           a.radius0, vball + dg * words, a);
+        const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
+        if (lane == 0) {
+            atomicAdd(&counters[0], 32u);
+            if (nm) atomicAdd(&counters[1], (unsigned)__popc(nm));
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x;
+    const int words = a.g.words;
+    const bool split = a.vbits != nullptr;
+    wait_primary_grid();   // the previous step's state (programmatic launch)
+    const int i0 = (int)(blockIdx.x >> a.chunk_shift) * kGroup;
+    const int G = min(kGroup, a.n - i0);
+    int j0 = 0, n = a.n;   // neighbours are [j0, n)
+    if (split) {
+        j0 = (int)(blockIdx.x & ((1u << a.chunk_shift) - 1u)) * a.chunk_len;
+        n = min(n, j0 + a.chunk_len);
+    }
+    uint32_t *vball = reinterpret_cast<uint32_t *>(smem);
+    size_t off = ((size_t)kGroup * words * 4 + 15) & ~size_t(15);
+    FocalDev *fd = reinterpret_cast<FocalDev *>(smem + off);
+    off += ((size_t)kGroup * sizeof(FocalDev) + 15) & ~size_t(15);
+    QEntry<false> *q = reinterpret_cast<QEntry<false> *>(smem + off);
+    QEntry<false> *q2 = q + kQueue;
+    off += (size_t)(kQueue + kQueue2) * sizeof(QEntry<false>);
+    int2 *wq = reinterpret_cast<int2 *>(smem + off);
+    off += (size_t)kQueueW * sizeof(int2);
+    unsigned *counters = reinterpret_cast<unsigned *>(smem + off);
+
+    for (int w = lane; w < G * words; w += 32) vball[w] = 0u;
+    if (lane < 4) counters[lane] = 0u;
+    allow_dependent_launch();
+    if (lane < G) fd[lane] = load_focal<false>(a, i0 + lane);   // the group's agents at once
+    __syncwarp();
+    const float cull_r2 = a.radius0 * a.radius0 * a.g.cull;
+
+    int qn = 0, q2n = 0, wqn = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    // two adjacent neighbours per lane, 64 per round: one 8-byte load per coordinate when the
+    // state is 8-byte aligned (the pairs start at an even index)
+    const bool pl = a.pair_loads != 0;
+    auto load2 = [&](int jj, float2 &xv, float2 &yv) {
+        if (pl && jj + 1 < n) {
+            xv = __ldg(reinterpret_cast<const float2 *>(a.x + jj));
+            yv = __ldg(reinterpret_cast<const float2 *>(a.y + jj));
+        } else {
+            xv = make_float2(jj < n ? __ldg(a.x + jj) : 0.f, jj + 1 < n ? __ldg(a.x + jj + 1) : 0.f);
+            yv = make_float2(jj < n ? __ldg(a.y + jj) : 0.f, jj + 1 < n ? __ldg(a.y + jj + 1) : 0.f);
+        }
+    };
+    const int jb0 = j0 & ~1;
+    float2 xn2, yn2;
+    load2(jb0 + 2 * lane, xn2, yn2);
+    for (int jb = jb0; jb < n; jb += 64) {
+        const float2 xv = xn2, yv = yn2;
+        const int jj = jb + 2 * lane;
+        load2(jb + 64 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
+        const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
+        for (int g = 0; g < G; ++g) {   // warp-uniform
+            const float fx = fd[g].x, fy = fd[g].y;
+            const float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
+            const float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
+            const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+            const bool live0 = v0 && d2.x > 0.f && d2.x <= cull_r2;
+            const bool live1 = v1 && d2.y > 0.f && d2.y <= cull_r2;
+            const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
+            const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
+            const int c0 = __popc(lm0);
+            const int tag = jj | (g << kGroupTagShift);
+            if (live0) q[qn + __popc(lm0 & lt)] = QEntry<false>::make(dx.x, dy.x, d2.x, tag);
+            if (live1)
+                q[qn + c0 + __popc(lm1 & lt)] = QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1);
+            qn += c0 + __popc(lm1);
+            __syncwarp();
+            while (qn >= 32) {   // warp-uniform; at most two batches
+                qn -= 32;
+                group_batch<true>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a, counters);
+            }
+        }
+    }
+    if (qn > 0) group_batch<false>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
+    if (lane < wqn) {   // the last long or wrapping runs
+        const int2 r = wq[lane];
+        raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
+                          r.y & ((1 << kGroupTagShift) - 1));
+    }
+    __syncwarp();
+    bool near = false;   // the last (< 32) deferred pairs
+    if (lane < q2n) {
+        const int tag = q2[lane].j();
+        const int dg = (int)((unsigned)tag >> kGroupTagShift);
+        const int j = tag & ((1 << kGroupTagShift) - 1);
+        near = resolve_and_raster<false, false>(fd[dg], __ldg(a.x + j), __ldg(a.y + j),
+                                                a.radius0, vball + dg * words, a);
+    }
+    const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
+    if (lane == 0 && q2n) {
+        counters[0] += (unsigned)q2n;
+        counters[1] += (unsigned)__popc(nm);
+    }
+    __syncwarp();
+    if (split) {   // the group's partial bitmasks (consecutive agents) into the workspace
+        uint32_t *gb = a.vbits + (size_t)i0 * words;
+        for (int w = lane; w < G * words; w += 32) {
+            const uint32_t v = vball[w];
+            if (v) atomicOr(gb + w, v);
+        }
+    } else {       // integrals of each agent (the drained queues hold its transition list)
+        for (int g = 0; g < G; ++g)
+            finish_agent(a, i0 + g, vball + g * words, reinterpret_cast<uint32_t *>(q),
+                         kListCap<false>);
+    }
+    if (lane == 0) flush_counters(a, counters);
+}
+
 // ---------------------------------------------------------------------------- tiled form
 // Several focal warps per block; neighbour tiles staged in shared memory by the TMA bulk
 // engine (double-buffered when the swarm spans more than one tile).
@@ -1033,6 +1216,32 @@ static int launch_l1(StepArgs a, int wpa, int split, cudaStream_t stream, int *c
     return check_cuda(e, "vpf_pairs_l1_kernel launch");
 }
 
+// group form (walls, equal radii, one swarm): chunks as in launch_l1, counted in groups.
+static int launch_group(StepArgs a, int split, cudaStream_t stream, int *chunks) {
+    const size_t smem = group_smem_bytes(a.g.words);
+    const int groups = (a.n + kGroup - 1) / kGroup;
+    int c = 1;
+    if (a.vbits) {
+        if (split > 0) {
+            c = split;
+        } else {
+            // about two waves of resident blocks (measured best at N=4096: 8 chunks, 8192
+            // blocks; 4 chunks and 16 chunks were 2 us and 4 us slower per step)
+            const long slots = resident_slots((const void *)vpf_pairs_group_kernel, 32, smem);
+            while (c < 16 && (long)groups * 2 * c <= 2 * slots && a.n / (2 * c) >= 256) c *= 2;
+        }
+    }
+    int shift = 0;
+    while ((1 << shift) < c) ++shift;
+    a.chunk_shift = shift;
+    a.chunk_len = c > 1 ? ((a.n + c - 1) / c + 63) / 64 * 64 : a.n;
+    if (c == 1) a.vbits = nullptr;
+    *chunks = c;
+    const unsigned blocks = (unsigned)groups << shift;
+    return check_cuda(launch_pdl(vpf_pairs_group_kernel, blocks, 32, smem, stream, a),
+                      "vpf_pairs_group_kernel launch");
+}
+
 template <bool TORUS, bool HETERO, bool TMA>
 static int launch_tiled(const StepArgs &a, int warps, cudaStream_t stream) {
     auto kern = vpf_pairs_tiled_kernel<TORUS, HETERO, TMA>;
@@ -1299,7 +1508,7 @@ int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile) {
 
 int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent) {
     std::lock_guard<std::mutex> lk(g_cfg_mu);
-    if (mode < 0 || mode > 2) return set_error(ABM_ERR_INVALID_ARG, "mode=%d", mode);
+    if (mode < 0 || mode > 3) return set_error(ABM_ERR_INVALID_ARG, "mode=%d", mode);
     if (warps_per_agent && warps_per_agent != 1 && warps_per_agent != 2 && warps_per_agent != 4)
         return set_error(ABM_ERR_INVALID_ARG, "warps_per_agent=%d", warps_per_agent);
     g_mode = mode;
@@ -1375,9 +1584,16 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     const bool hetero = a.radius != nullptr;
     // auto: the l1 form while the positions fit comfortably in L1, tiled beyond; segmented
     // (batched) swarms always use the l1 form
-    const bool use_l1 = seg_begin || mode == 1 || (mode == 0 && n <= 16384);
+    const bool group_ok = !seg_begin && !torus && !hetero && n < (1 << kGroupTagShift);
+    if (mode == 3 && !group_ok)
+        return set_error(ABM_ERR_UNSUPPORTED, "%s: the group form needs one swarm with walls and "
+                                              "equal radii", fn);
+    const bool use_group = group_ok && (mode == 3 || (mode == 0 && n <= 16384));
+    const bool use_l1 = !use_group && (seg_begin || mode == 1 || (mode == 0 && n <= 16384));
     int chunks = 1;
-    if (use_l1) {
+    if (use_group) {
+        st = launch_group(a, split, s, &chunks);
+    } else if (use_l1) {
         if (!torus && !hetero) st = launch_l1<false, false>(a, wpa, split, s, &chunks);
         else if (!torus && hetero) st = launch_l1<false, true>(a, wpa, split, s, &chunks);
         else if (torus && !hetero) st = launch_l1<true, false>(a, wpa, split, s, &chunks);

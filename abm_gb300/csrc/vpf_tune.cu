@@ -19,6 +19,7 @@ static std::vector<abm_step_config> tune_candidates(bool segmented) {
         return c;
     }
     const int chunks[] = {1, 2, 4, 8, 16};
+    for (int ch : chunks) c.push_back({3, 1, ch, 8, 8192, -1.f});   // group form (if it applies)
     for (int wpa : wpas)
         for (int ch : chunks) c.push_back({1, wpa, ch, 8, 8192, -1.f});
     const int warps[] = {4, 8, 16};

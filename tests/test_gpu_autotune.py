@@ -51,7 +51,7 @@ def test_autotune_single_swarm(restore_config):
     s = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
     res = autotune.tune(s, reps=2)
     tried = res["tried"]
-    assert len(tried) == 27
+    assert len(tried) == 32   # 5 group-form + 15 L1-form + 12 tiled-form candidates
     ran = [t for t in tried if t["ms_per_step"] > 0]
     assert ran, tried
     best = res["best"]

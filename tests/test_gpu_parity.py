@@ -202,17 +202,29 @@ def _configs_agree(vp, st, configs, radius=None):
 def test_launch_configs_agree():
     """Every kernel form and launch configuration gives bit-identical results: the L1 form
     with 1, 2 and 4 warps per agent, one block per agent or the neighbours split over 2-16
-    blocks (partial bitmasks OR-ed in the workspace, integrals in the finish kernel), and the
-    TMA-tiled form with several (warps per block, tile) shapes including multi-tile double
-    buffering."""
+    blocks (partial bitmasks OR-ed in the workspace, integrals in the finish kernel), the
+    group form (one warp for 4 agents) with 1-16 chunks, and the TMA-tiled form with several
+    (warps per block, tile) shapes including multi-tile double buffering."""
     from abm_gb300.params import VFParams
     st = seeded_swarm(5, 1000, 2000.0, 2000.0, R=5.0)
     vp = VFParams(width=2000.0, height=2000.0, rv=1200, radius=5.0)
     _configs_agree(vp, st, ((1, 1, 8, 8192, 1), (1, 2, 8, 8192, 1), (1, 4, 8, 8192, 1),
                             (1, 1, 8, 8192, 2), (1, 1, 8, 8192, 4), (1, 1, 8, 8192, 16),
                             (1, 2, 8, 8192, 8), (1, 4, 8, 8192, 4), (0, 1, 8, 8192, 0),
+                            (3, 1, 8, 8192, 1), (3, 1, 8, 8192, 2), (3, 1, 8, 8192, 8),
+                            (3, 1, 8, 8192, 16),
                             (2, 1, 8, 2048, 0), (2, 1, 4, 256, 0), (2, 1, 16, 1024, 0),
                             (2, 1, 32, 64, 0), (2, 1, 1, 4096, 0)))
+
+
+def test_group_form_partial_last_group():
+    """1003 agents (a last group of 3) and a swarm of 3 (one partial group): the group form
+    with and without chunks equals the L1 form."""
+    from abm_gb300.params import VFParams
+    for n, W in ((1003, 2000.0), (3, 200.0)):
+        st = seeded_swarm(15, n, W, W, R=5.0)
+        vp = VFParams(width=W, height=W, rv=1200, radius=5.0)
+        _configs_agree(vp, st, ((1, 1, 8, 8192, 1), (3, 1, 8, 8192, 1), (3, 1, 8, 8192, 4)))
 
 
 def test_launch_configs_agree_torus_radii():
