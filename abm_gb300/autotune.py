@@ -1,7 +1,8 @@
 """Launch-configuration autotuner of the step (abm_vpf_autotune).
 
-``tune(obj)`` times every candidate configuration of the step — the L1 form with 1, 2 or 4
-warps per focal agent and 1-16 neighbour chunks, the tiled form with several agents-per-block
+``tune(obj)`` times every candidate configuration of the step — the group form (4 focal
+agents per warp) and the L1 form with 1, 2 or 4 warps per focal agent, each with 1-16
+neighbour chunks, the tiled form with several agents-per-block
 and tile lengths; for a batched sweep the L1 form with 1, 2 or 4 warps per agent — on the
 object's own current state and stream, applies the fastest, and returns it with the whole
 table.  All configurations give bit-identical results.  ``apply(config)`` re-applies a

@@ -1,7 +1,8 @@
 // vpf_tune.cu -- autotuner of the step's launch configuration (abm_vpf_autotune).
 //
-// Every form of the step (L1 form with 1, 2 or 4 warps per focal agent and 1-16 neighbour
-// chunks, tiled form with several agents-per-block and tile lengths) gives bit-identical
+// Every form of the step (group form with 1-16 neighbour chunks, L1 form with 1, 2 or 4 warps
+// per focal agent and 1-16 neighbour chunks, tiled form with several agents-per-block and tile
+// lengths) gives bit-identical
 // results, so the best one for a workload is an empirical question: the tuner times each
 // candidate on the caller's own state and stream and applies the fastest.
 #include <vector>

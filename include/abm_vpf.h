@@ -381,17 +381,20 @@ int abm_vpf_edge_bwd_f64(const abm_swarm_state_f64 *in, const abm_swarm_state_f6
 int abm_vpf_set_step_config(int32_t warps_per_block, int32_t tile);
 int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile);
 
-/* Form of the pair kernel of abm_vpf_flock_step: mode 0 = automatic (the L1 form up to 16384
- * agents, the tiled form beyond), 1 = L1 form (one block per focal agent, neighbours read
- * through the read-only L1 path), 2 = tiled form (warps_per_block focal agents share
- * TMA-staged neighbour tiles).  warps_per_agent in {1, 2, 4} splits one focal agent's
- * neighbours over that many warps in the L1 form; 0 keeps the current value.  All forms give
- * bit-identical results. */
+/* Form of the pair kernel of abm_vpf_flock_step: mode 0 = automatic (up to 16384 agents the
+ * group form where it applies, else the L1 form; the tiled form beyond), 1 = L1 form (one
+ * block per focal agent, neighbours read through the read-only L1 path), 2 = tiled form
+ * (warps_per_block focal agents share TMA-staged neighbour tiles), 3 = group form (one warp
+ * per group of 4 consecutive focal agents, each neighbour read once for the group; one swarm
+ * with walls and equal radii only, otherwise the step returns ABM_ERR_UNSUPPORTED).
+ * warps_per_agent in {1, 2, 4} splits one focal agent's neighbours over that many warps in the
+ * L1 form; 0 keeps the current value.  All forms give bit-identical results. */
 int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent);
 int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent);
 
-/* Neighbour chunks per focal agent in the L1 form of abm_vpf_flock_step (not the batched or
- * no-alloc calls): with chunks > 1 each agent's neighbours are split over that many blocks,
+/* Neighbour chunks per focal agent in the L1 and group forms of abm_vpf_flock_step (not the
+ * batched or no-alloc calls): with chunks > 1 each agent's neighbours are split over that many
+ * blocks,
  * whose partial bitmasks are OR-ed into a per-agent bitmask in the stream's workspace (Rv/8
  * bytes per agent) and reduced by a second kernel, so that the block scheduler can balance the
  * SMs' work when the swarm alone does not fill the GPU several times over.  0 (the default) =
@@ -401,9 +404,9 @@ int abm_vpf_get_step_split(int32_t *chunks);
 
 /* One launch configuration of the step and its measured time. */
 typedef struct {
-    int32_t mode;              /* 1 = L1 form, 2 = tiled form */
+    int32_t mode;              /* 1 = L1 form, 2 = tiled form, 3 = group form */
     int32_t warps_per_agent;   /* L1 form: warps sharing one focal agent (1, 2, 4) */
-    int32_t chunks;            /* L1 form, single swarm: neighbour chunks per agent (1..16) */
+    int32_t chunks;            /* L1 / group form, single swarm: neighbour chunks (1..16) */
     int32_t warps_per_block;   /* tiled form: focal agents per block */
     int32_t tile;              /* tiled form: neighbour tile length */
     float ms_per_step;         /* mean device time of one step; < 0 if the form was refused */
@@ -413,8 +416,9 @@ typedef struct {
  * Autotuner (no counterpart in the reference): times the step on the caller's own state and
  * stream under every candidate configuration and applies the fastest one through
  * abm_vpf_set_step_mode / _config / _split.  Candidates for a single swarm (seg_begin_dev ==
- * NULL): the L1 form with warps_per_agent in {1, 2, 4} x chunks in {1, 2, 4, 8, 16}, and the
- * tiled form with warps_per_block in {4, 8, 16} x tile in {1024, 2048, 4096, 8192}; for a
+ * NULL): the group form with chunks in {1, 2, 4, 8, 16} (refused where it does not apply), the
+ * L1 form with warps_per_agent in {1, 2, 4} x chunks in {1, 2, 4, 8, 16}, and the tiled form
+ * with warps_per_block in {4, 8, 16} x tile in {1024, 2048, 4096, 8192}; for a
  * batched sweep (segment arrays as for abm_vpf_flock_batched): the L1 form with
  * warps_per_agent in {1, 2, 4}.  Each candidate runs one untimed step and then `reps` timed
  * steps (CUDA events on `stream`) from `in` into a scratch state allocated by the call.  All
