@@ -654,16 +654,19 @@ __device__ __forceinline__ void group_batch(const FocalDev *fd, const QEntry<fal
 
 __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_agent[kGroup], s_j0[kGroup], s_j1[kGroup];
     const int lane = threadIdx.x;
     const int words = a.g.words;
     const bool split = a.vbits != nullptr;
     wait_primary_grid();   // the previous step's state (programmatic launch)
-    const int i0 = (int)(blockIdx.x >> a.chunk_shift) * kGroup;
-    const int G = min(kGroup, a.n - i0);
-    int j0 = 0, n = a.n;   // neighbours are [j0, n)
+    // the group: positions [p0, p0 + G) of the agent order (a batched sweep's schedule, else
+    // the agents themselves); neighbours of a single swarm: the block's chunk
+    const int p0 = (int)(blockIdx.x >> a.chunk_shift) * kGroup;
+    const int G = min(kGroup, a.n - p0);
+    int cj0 = 0, cj1 = a.n;
     if (split) {
-        j0 = (int)(blockIdx.x & ((1u << a.chunk_shift) - 1u)) * a.chunk_len;
-        n = min(n, j0 + a.chunk_len);
+        cj0 = (int)(blockIdx.x & ((1u << a.chunk_shift) - 1u)) * a.chunk_len;
+        cj1 = min(cj1, cj0 + a.chunk_len);
     }
     uint32_t *vball = reinterpret_cast<uint32_t *>(smem);
     size_t off = ((size_t)kGroup * words * 4 + 15) & ~size_t(15);
@@ -679,51 +682,69 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     for (int w = lane; w < G * words; w += 32) vball[w] = 0u;
     if (lane < 4) counters[lane] = 0u;
     allow_dependent_launch();
-    if (lane < G) fd[lane] = load_focal<false>(a, i0 + lane);   // the group's agents at once
+    if (lane < G) {   // the group's agents at once
+        const int i = a.order ? a.order[p0 + lane] : p0 + lane;
+        s_agent[lane] = i;
+        s_j0[lane] = a.seg_begin ? a.seg_begin[i] : cj0;
+        s_j1[lane] = a.seg_end ? a.seg_end[i] : cj1;
+        fd[lane] = load_focal<false>(a, i);
+    }
     __syncwarp();
     const float cull_r2 = a.radius0 * a.radius0 * a.g.cull;
 
     int qn = 0, q2n = 0, wqn = 0;
     const unsigned lt = (1u << lane) - 1u;
-    // two adjacent neighbours per lane, 64 per round: one 8-byte load per coordinate when the
-    // state is 8-byte aligned (the pairs start at an even index)
     const bool pl = a.pair_loads != 0;
-    auto load2 = [&](int jj, float2 &xv, float2 &yv) {
-        if (pl && jj + 1 < n) {
-            xv = __ldg(reinterpret_cast<const float2 *>(a.x + jj));
-            yv = __ldg(reinterpret_cast<const float2 *>(a.y + jj));
-        } else {
-            xv = make_float2(jj < n ? __ldg(a.x + jj) : 0.f, jj + 1 < n ? __ldg(a.x + jj + 1) : 0.f);
-            yv = make_float2(jj < n ? __ldg(a.y + jj) : 0.f, jj + 1 < n ? __ldg(a.y + jj + 1) : 0.f);
-        }
-    };
-    const int jb0 = j0 & ~1;
-    float2 xn2, yn2;
-    load2(jb0 + 2 * lane, xn2, yn2);
-    for (int jb = jb0; jb < n; jb += 64) {
-        const float2 xv = xn2, yv = yn2;
-        const int jj = jb + 2 * lane;
-        load2(jb + 64 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
-        const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
-        for (int g = 0; g < G; ++g) {   // warp-uniform
-            const float fx = fd[g].x, fy = fd[g].y;
-            const float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
-            const float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
-            const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
-            const bool live0 = v0 && d2.x > 0.f && d2.x <= cull_r2;
-            const bool live1 = v1 && d2.y > 0.f && d2.y <= cull_r2;
-            const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
-            const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
-            const int c0 = __popc(lm0);
-            const int tag = jj | (g << kGroupTagShift);
-            if (live0) q[qn + __popc(lm0 & lt)] = QEntry<false>::make(dx.x, dy.x, d2.x, tag);
-            if (live1)
-                q[qn + c0 + __popc(lm1 & lt)] = QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1);
-            qn += c0 + __popc(lm1);
-            __syncwarp();
-            while (qn >= 32) {   // warp-uniform; at most two batches
-                qn -= 32;
-                group_batch<true>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a, counters);
+    // one scan per distinct neighbour range of the group's agents (one for a single swarm; a
+    // group may straddle instances of a batched sweep)
+    unsigned todo = (1u << G) - 1u;
+    while (todo) {
+        const int gr = __ffs(todo) - 1;
+        const int j0 = s_j0[gr], n = s_j1[gr];
+        unsigned members = 0u;
+        for (int g = 0; g < G; ++g)
+            if (s_j0[g] == j0 && s_j1[g] == n) members |= 1u << g;
+        todo &= ~members;
+        // two adjacent neighbours per lane, 64 per round: one 8-byte load per coordinate when
+        // the state is 8-byte aligned (the pairs start at an even index)
+        auto load2 = [&](int jj, float2 &xv, float2 &yv) {
+            if (pl && jj + 1 < n) {
+                xv = __ldg(reinterpret_cast<const float2 *>(a.x + jj));
+                yv = __ldg(reinterpret_cast<const float2 *>(a.y + jj));
+            } else {
+                xv = make_float2(jj < n ? __ldg(a.x + jj) : 0.f, jj + 1 < n ? __ldg(a.x + jj + 1) : 0.f);
+                yv = make_float2(jj < n ? __ldg(a.y + jj) : 0.f, jj + 1 < n ? __ldg(a.y + jj + 1) : 0.f);
+            }
+        };
+        const int jb0 = j0 & ~1;
+        float2 xn2, yn2;
+        load2(jb0 + 2 * lane, xn2, yn2);
+        for (int jb = jb0; jb < n; jb += 64) {
+            const float2 xv = xn2, yv = yn2;
+            const int jj = jb + 2 * lane;
+            load2(jb + 64 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
+            const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
+            for (int g = 0; g < G; ++g) {   // warp-uniform
+                if (!((members >> g) & 1u)) continue;
+                const float fx = fd[g].x, fy = fd[g].y;
+                const float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
+                const float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
+                const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+                const bool live0 = v0 && d2.x > 0.f && d2.x <= cull_r2;
+                const bool live1 = v1 && d2.y > 0.f && d2.y <= cull_r2;
+                const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
+                const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
+                const int c0 = __popc(lm0);
+                const int tag = jj | (g << kGroupTagShift);
+                if (live0) q[qn + __popc(lm0 & lt)] = QEntry<false>::make(dx.x, dy.x, d2.x, tag);
+                if (live1)
+                    q[qn + c0 + __popc(lm1 & lt)] = QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1);
+                qn += c0 + __popc(lm1);
+                __syncwarp();
+                while (qn >= 32) {   // warp-uniform; at most two batches
+                    qn -= 32;
+                    group_batch<true>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a, counters);
+                }
             }
         }
     }
@@ -749,14 +770,14 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     }
     __syncwarp();
     if (split) {   // the group's partial bitmasks (consecutive agents) into the workspace
-        uint32_t *gb = a.vbits + (size_t)i0 * words;
+        uint32_t *gb = a.vbits + (size_t)p0 * words;
         for (int w = lane; w < G * words; w += 32) {
             const uint32_t v = vball[w];
             if (v) atomicOr(gb + w, v);
         }
     } else {       // integrals of each agent (the drained queues hold its transition list)
         for (int g = 0; g < G; ++g)
-            finish_agent(a, i0 + g, vball + g * words, reinterpret_cast<uint32_t *>(q),
+            finish_agent(a, s_agent[g], vball + g * words, reinterpret_cast<uint32_t *>(q),
                          kListCap<false>);
     }
     if (lane == 0) flush_counters(a, counters);
@@ -1584,11 +1605,12 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     const bool hetero = a.radius != nullptr;
     // auto: the l1 form while the positions fit comfortably in L1, tiled beyond; segmented
     // (batched) swarms always use the l1 form
-    const bool group_ok = !seg_begin && !torus && !hetero && n < (1 << kGroupTagShift);
+    const bool group_ok = !torus && !hetero && n < (1 << kGroupTagShift);
     if (mode == 3 && !group_ok)
-        return set_error(ABM_ERR_UNSUPPORTED, "%s: the group form needs one swarm with walls and "
-                                              "equal radii", fn);
-    const bool use_group = group_ok && (mode == 3 || (mode == 0 && n <= 16384));
+        return set_error(ABM_ERR_UNSUPPORTED, "%s: the group form needs walls and equal radii",
+                         fn);
+    // automatic: the group form for one swarm up to 16384 agents and for batched sweeps
+    const bool use_group = group_ok && (mode == 3 || (mode == 0 && (seg_begin || n <= 16384)));
     const bool use_l1 = !use_group && (seg_begin || mode == 1 || (mode == 0 && n <= 16384));
     int chunks = 1;
     if (use_group) {

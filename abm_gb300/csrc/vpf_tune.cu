@@ -16,6 +16,7 @@ static std::vector<abm_step_config> tune_candidates(bool segmented) {
     std::vector<abm_step_config> c;
     const int wpas[] = {1, 2, 4};
     if (segmented) {
+        c.push_back({3, 1, 1, 8, 8192, -1.f});   // group form (if it applies)
         for (int wpa : wpas) c.push_back({1, wpa, 1, 8, 8192, -1.f});
         return c;
     }

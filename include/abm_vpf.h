@@ -174,7 +174,9 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
  * override arrays.  order_dev (nullable): a permutation of [0, n_total) giving the order in which
  * agents are scheduled (put the largest instances first for load balance).  All instances share
  * p (Rv, arena, boundary, GAM, ALP1, BET1 ...).  Results per instance are bit-identical to
- * abm_vpf_flock_step on that instance alone.  Always uses the L1 form of the pair kernel.
+ * abm_vpf_flock_step on that instance alone.  Uses the group form of the pair kernel (groups
+ * of 4 consecutive entries of the order) where it applies (walls, equal radii) and the L1 form
+ * otherwise, unless abm_vpf_set_step_mode selects one.
  */
 int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32_t n_total,
                           const int32_t *seg_begin_dev, const int32_t *seg_end_dev,
@@ -419,8 +421,8 @@ typedef struct {
  * NULL): the group form with chunks in {1, 2, 4, 8, 16} (refused where it does not apply), the
  * L1 form with warps_per_agent in {1, 2, 4} x chunks in {1, 2, 4, 8, 16}, and the tiled form
  * with warps_per_block in {4, 8, 16} x tile in {1024, 2048, 4096, 8192}; for a
- * batched sweep (segment arrays as for abm_vpf_flock_batched): the L1 form with
- * warps_per_agent in {1, 2, 4}.  Each candidate runs one untimed step and then `reps` timed
+ * batched sweep (segment arrays as for abm_vpf_flock_batched): the group form and the L1 form
+ * with warps_per_agent in {1, 2, 4}.  Each candidate runs one untimed step and then `reps` timed
  * steps (CUDA events on `stream`) from `in` into a scratch state allocated by the call.  All
  * configurations give bit-identical results, so tuning changes only the speed.  Synchronises
  * the stream; must not be called during stream capture.  best: the chosen configuration;

@@ -83,8 +83,9 @@ def test_autotune_batched_sweep(restore_config):
     b = BatchedSweep(vp, inst)
     before = {k: t.clone() for k, t in b._bufs[b._cur].items()}
     res = autotune.tune(b, reps=2)
-    assert len(res["tried"]) == 3
-    assert all(t["mode"] == 1 and t["chunks"] == 1 for t in res["tried"])
+    assert len(res["tried"]) == 4   # the group form, and the L1 form with 1, 2, 4 warps
+    assert [t["mode"] for t in res["tried"]] == [3, 1, 1, 1]
+    assert all(t["chunks"] == 1 for t in res["tried"])
     for k, t in before.items():
         assert bool((b._bufs[b._cur][k] == t).all())
     assert _current(lib)["warps_per_agent"] == res["best"]["warps_per_agent"]

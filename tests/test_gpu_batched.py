@@ -54,6 +54,36 @@ def test_batched_step_matches_single_instances():
             assert np.array_equal(st[key], bs[key]), (k, key)
 
 
+def test_batched_group_and_l1_forms_agree():
+    """The group form (4 consecutive entries of the schedule per warp, straddling instances)
+    and the L1 form give identical results for a sweep, also with a schedule that interleaves
+    the instances' agents."""
+    import torch
+    from abm_gb300 import _lib
+    from abm_gb300.batched import BatchedSweep
+    from abm_gb300.params import VFParams
+    lib = _lib.load()
+    vp = VFParams(alp1=0.08, bet1=0.08, width=600.0, height=600.0, rv=1200)
+    inst = _instances(seed=21)
+    outs = []
+    try:
+        for mode, shuffle in ((1, False), (3, False), (3, True)):
+            _lib.check(lib.abm_vpf_set_step_mode(mode, 1))
+            b = BatchedSweep(vp, inst)
+            if shuffle:   # a schedule whose groups of 4 mix agents of several instances
+                perm = np.random.default_rng(2).permutation(b.n).astype(np.int32)
+                b.order = torch.as_tensor(perm, device="cuda")
+            b.step(want_vpf=True, want_terms=True)
+            outs.append((b.vpf_numpy(), b.terms.cpu().numpy(), b.state_numpy()))
+    finally:
+        lib.abm_vpf_set_step_mode(0, 1)
+    for o in outs[1:]:
+        assert np.array_equal(o[0], outs[0][0])
+        assert np.array_equal(o[1], outs[0][1])
+        for k in o[2]:
+            assert np.array_equal(o[2][k], outs[0][2][k])
+
+
 def test_batched_small_instances_vs_oracle():
     from abm_gb300.batched import BatchedSweep
     from abm_gb300.params import VFParams
