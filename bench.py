@@ -49,10 +49,10 @@ WORKLOAD = dict(workload="vf_large_swarm", n_agents=4096, radius=5.0, arena=[500
 # agent: F = 36 (N-1) + 4 Rv + 20, M = 3 (N-1).
 F_PAIR, F_PX, F_UPD, M_PAIR = 36, 4, 20, 3
 L2_FLUSH_BYTES = 256 << 20
-# DRAM traffic of one launch of the dominant kernel (the pair kernel) of this workload, from the
-# ncu capture summarised in profiles/vpf_pairs_l1_n4096_rv3600.md
+# DRAM traffic of one launch of the dominant kernel (the group-form pair kernel) of this
+# workload, from the ncu capture summarised in profiles/vpf_pairs_group_n4096_rv3600.md
 # (dram__bytes_read.sum + dram__bytes_write.sum).
-NCU_TRAFFIC_BYTES = 2018816
+NCU_TRAFFIC_BYTES = 2022144
 
 
 def make_workload(seed=WORKLOAD["seed"], n=WORKLOAD["n_agents"]):
@@ -710,6 +710,29 @@ def run_gb300(args, rank, world):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     from abm_gb300 import autotune
     tuned = autotune.tune(sw, reps=5)   # launch configuration of the step, before any timing
+    # The tuner times back-to-back steps with the state warm in L2; the timed region below
+    # flushes L2 before every step.  Its best three candidates and the library's automatic
+    # choice are timed again under those conditions, and the fastest is used.
+    ran = sorted([t for t in tuned["tried"] if t["ms_per_step"] > 0],
+                 key=lambda t: t["ms_per_step"])[:3]
+    finalists = [dict(DEFAULT_STEP_CONFIG, chosen="automatic")] + [dict(t) for t in ran]
+    for cfg in finalists:
+        autotune.apply(cfg)
+        for _ in range(3):
+            sw.step()
+        evs = []
+        for k in range(20):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sw.step()
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        cfg["ms_per_step_l2_flushed"] = float(np.mean([a.elapsed_time(c) for a, c in evs]))
+    chosen = min(finalists, key=lambda c: c["ms_per_step_l2_flushed"])
+    autotune.apply(chosen)
+    sw.set_state(state["x"], state["y"], state["theta"], state["v"])
 
     peaks = measure_peaks(lib, torch, stream)
     for _ in range(args.warmup):
@@ -805,7 +828,8 @@ def run_gb300(args, rank, world):
                 "frac": achieved / peak,
                 "traffic": NCU_TRAFFIC_BYTES,
                 "timed": "whole step on the launching stream: the pair kernel and its "
-                         "dependent finish kernel (the pair kernel is ~86 % of it)",
+                         "dependent finish kernel (the group-form pair kernel is ~83 % of the "
+                         "serialised launch list)",
                 "algorithmic": {"fp32_ops_per_launch": F, "mufu_ops_per_launch": M,
                                 "fp32_frac": frac_f, "mufu_frac": frac_m,
                                 "hbm_bytes_per_launch": n * 32},
@@ -836,8 +860,14 @@ def run_gb300(args, rank, world):
             # pair kernel + finish (or update) kernel per step, in every timed sequence
             "gpu_launches": 2 * args.steps * len(reps_k),
             "roofline": roofline, "clocks": clk,
-            "launch_config": dict(tuned["best"], chosen_by="abm_vpf_autotune, 5 steps per "
-                                  "candidate", candidates=len(tuned["tried"]),
+            "launch_config": dict(chosen, chosen_by="abm_vpf_autotune (5 back-to-back steps "
+                                  "per candidate), then its best three and the automatic "
+                                  "choice timed over 20 steps with the L2 flushed before each",
+                                  candidates=len(tuned["tried"]),
+                                  finalists=[{k: f[k] for k in ("mode", "warps_per_agent",
+                                                                "chunks",
+                                                                "ms_per_step_l2_flushed")}
+                                             for f in finalists],
                                   table=compact_table(tuned["tried"])),
             "wall_s_timed_region": t_wall,
             "diagnostics": diag}
@@ -860,7 +890,15 @@ def profile_workload(which: str):
     """A few eager steps of one leg's workload and nothing else: the command the ncu
     summaries under profiles/ capture (launch lists and single-kernel captures)."""
     import torch
-    if which == "batched":
+    if which == "headline":
+        from abm_gb300.swarm import VFSwarm
+        st = make_workload()
+        sw = VFSwarm(make_params(), st["x"], st["y"], st["theta"], st["v"])
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+        for k in range(10):   # as in the timed region: the L2 flushed before every step
+            flush.fill_(float(k))
+            sw.step()
+    elif which == "batched":
         from abm_gb300.batched import BatchedSweep, sweep_instances
         from abm_gb300.params import VFParams
         B = BATCHED
@@ -907,7 +945,8 @@ def main():
     ap.add_argument("--min-device-s", type=float, default=1.0,
                     help="repeat the timed K-step sequence until this much step time")
     ap.add_argument("--max-repeats", type=int, default=2000)
-    ap.add_argument("--profile-workload", choices=["batched", "forage", "forage_collide", "edge"],
+    ap.add_argument("--profile-workload",
+                    choices=["headline", "batched", "forage", "forage_collide", "edge"],
                     help="run a few eager steps of one leg's workload and exit (for ncu)")
     args = ap.parse_args()
     if args.profile_workload:
