@@ -37,6 +37,16 @@ __device__ __forceinline__ void wait_primary_grid() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
+// The calling grid's share of the 128-byte lines of a read-only table, prefetched into L2
+// (each thread of the grid takes lines tid, tid + grid threads, ...; only lines inside
+// [base, base + bytes) are touched).
+__device__ __forceinline__ void prefetch_table_l2(const void *base, size_t bytes) {
+    const size_t lines = (bytes + 127) / 128;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < lines; l += stride)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"((const char *)base + l * 128));
+}
+
 // ------------------------------------------------------------------ double-float arithmetic
 struct dfl {
     float hi, lo;

@@ -652,7 +652,124 @@ __device__ __forceinline__ void group_batch(const FocalDev *fd, const QEntry<fal
     }
 }
 
+// The group form for one swarm: the group is 4 consecutive agents, the neighbours the block's
+// chunk.
 __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x;
+    const int words = a.g.words;
+    const bool split = a.vbits != nullptr;
+    wait_primary_grid();   // the previous step's state (programmatic launch)
+    const int i0 = (int)(blockIdx.x >> a.chunk_shift) * kGroup;
+    const int G = min(kGroup, a.n - i0);
+    int j0 = 0, n = a.n;   // neighbours are [j0, n)
+    if (split) {
+        j0 = (int)(blockIdx.x & ((1u << a.chunk_shift) - 1u)) * a.chunk_len;
+        n = min(n, j0 + a.chunk_len);
+    }
+    uint32_t *vball = reinterpret_cast<uint32_t *>(smem);
+    size_t off = ((size_t)kGroup * words * 4 + 15) & ~size_t(15);
+    FocalDev *fd = reinterpret_cast<FocalDev *>(smem + off);
+    off += ((size_t)kGroup * sizeof(FocalDev) + 15) & ~size_t(15);
+    QEntry<false> *q = reinterpret_cast<QEntry<false> *>(smem + off);
+    QEntry<false> *q2 = q + kQueue;
+    off += (size_t)(kQueue + kQueue2) * sizeof(QEntry<false>);
+    int2 *wq = reinterpret_cast<int2 *>(smem + off);
+    off += (size_t)kQueueW * sizeof(int2);
+    unsigned *counters = reinterpret_cast<unsigned *>(smem + off);
+
+    for (int w = lane; w < G * words; w += 32) vball[w] = 0u;
+    if (lane < 4) counters[lane] = 0u;
+    allow_dependent_launch();
+    if (lane < G) fd[lane] = load_focal<false>(a, i0 + lane);   // the group's agents at once
+    __syncwarp();
+    const float cull_r2 = a.radius0 * a.radius0 * a.g.cull;
+
+    int qn = 0, q2n = 0, wqn = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    // two adjacent neighbours per lane, 64 per round: one 8-byte load per coordinate when the
+    // state is 8-byte aligned (the pairs start at an even index)
+    const bool pl = a.pair_loads != 0;
+    auto load2 = [&](int jj, float2 &xv, float2 &yv) {
+        if (pl && jj + 1 < n) {
+            xv = __ldg(reinterpret_cast<const float2 *>(a.x + jj));
+            yv = __ldg(reinterpret_cast<const float2 *>(a.y + jj));
+        } else {
+            xv = make_float2(jj < n ? __ldg(a.x + jj) : 0.f, jj + 1 < n ? __ldg(a.x + jj + 1) : 0.f);
+            yv = make_float2(jj < n ? __ldg(a.y + jj) : 0.f, jj + 1 < n ? __ldg(a.y + jj + 1) : 0.f);
+        }
+    };
+    const int jb0 = j0 & ~1;
+    float2 xn2, yn2;
+    load2(jb0 + 2 * lane, xn2, yn2);
+    for (int jb = jb0; jb < n; jb += 64) {
+        const float2 xv = xn2, yv = yn2;
+        const int jj = jb + 2 * lane;
+        load2(jb + 64 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
+        const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
+        for (int g = 0; g < G; ++g) {   // warp-uniform
+            const float fx = fd[g].x, fy = fd[g].y;
+            const float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
+            const float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
+            const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+            const bool live0 = v0 && d2.x > 0.f && d2.x <= cull_r2;
+            const bool live1 = v1 && d2.y > 0.f && d2.y <= cull_r2;
+            const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
+            const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
+            const int c0 = __popc(lm0);
+            const int tag = jj | (g << kGroupTagShift);
+            if (live0) q[qn + __popc(lm0 & lt)] = QEntry<false>::make(dx.x, dy.x, d2.x, tag);
+            if (live1)
+                q[qn + c0 + __popc(lm1 & lt)] = QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1);
+            qn += c0 + __popc(lm1);
+            __syncwarp();
+            while (qn >= 32) {   // warp-uniform; at most two batches
+                qn -= 32;
+                group_batch<true>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a, counters);
+            }
+        }
+    }
+    if (qn > 0) group_batch<false>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
+    if (lane < wqn) {   // the last long or wrapping runs
+        const int2 r = wq[lane];
+        raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
+                          r.y & ((1 << kGroupTagShift) - 1));
+    }
+    __syncwarp();
+    bool near = false;   // the last (< 32) deferred pairs
+    if (lane < q2n) {
+        const int tag = q2[lane].j();
+        const int dg = (int)((unsigned)tag >> kGroupTagShift);
+        const int j = tag & ((1 << kGroupTagShift) - 1);
+        near = resolve_and_raster<false, false>(fd[dg], __ldg(a.x + j), __ldg(a.y + j),
+                                                a.radius0, vball + dg * words, a);
+    }
+    const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
+    if (lane == 0 && q2n) {
+        counters[0] += (unsigned)q2n;
+        counters[1] += (unsigned)__popc(nm);
+    }
+    __syncwarp();
+    if (split) {   // the group's partial bitmasks (consecutive agents) into the workspace
+        uint32_t *gb = a.vbits + (size_t)i0 * words;
+        for (int w = lane; w < G * words; w += 32) {
+            const uint32_t v = vball[w];
+            if (v) atomicOr(gb + w, v);
+        }
+    } else {       // integrals of each agent (the drained queues hold its transition list)
+        for (int g = 0; g < G; ++g)
+            finish_agent(a, i0 + g, vball + g * words, reinterpret_cast<uint32_t *>(q),
+                         kListCap<false>);
+    }
+    if (lane == 0) flush_counters(a, counters);
+}
+
+// The group form for a batched sweep: the group is 4 consecutive entries of the schedule, and
+// each distinct neighbour range of its agents (a group may straddle instances) is scanned once
+// for the agents that share it.  (A separate kernel: folding this into the single-swarm kernel
+// measured 1.3 us slower per step at N=4096.)
+template <bool SEG>
+__global__ void __launch_bounds__(32) vpf_pairs_group_seg_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_agent[kGroup], s_j0[kGroup], s_j1[kGroup];
     const int lane = threadIdx.x;
@@ -683,10 +800,10 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     if (lane < 4) counters[lane] = 0u;
     allow_dependent_launch();
     if (lane < G) {   // the group's agents at once
-        const int i = a.order ? a.order[p0 + lane] : p0 + lane;
+        const int i = (SEG && a.order) ? a.order[p0 + lane] : p0 + lane;
         s_agent[lane] = i;
-        s_j0[lane] = a.seg_begin ? a.seg_begin[i] : cj0;
-        s_j1[lane] = a.seg_end ? a.seg_end[i] : cj1;
+        s_j0[lane] = SEG ? a.seg_begin[i] : cj0;
+        s_j1[lane] = SEG ? a.seg_end[i] : cj1;
         fd[lane] = load_focal<false>(a, i);
     }
     __syncwarp();
@@ -697,16 +814,10 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     const bool pl = a.pair_loads != 0;
     // one scan per distinct neighbour range of the group's agents (one for a single swarm; a
     // group may straddle instances of a batched sweep)
-    unsigned todo = (1u << G) - 1u;
-    while (todo) {
-        const int gr = __ffs(todo) - 1;
-        const int j0 = s_j0[gr], n = s_j1[gr];
-        unsigned members = 0u;
-        for (int g = 0; g < G; ++g)
-            if (s_j0[g] == j0 && s_j1[g] == n) members |= 1u << g;
-        todo &= ~members;
-        // two adjacent neighbours per lane, 64 per round: one 8-byte load per coordinate when
-        // the state is 8-byte aligned (the pairs start at an even index)
+    // one scan of a neighbour range [j0, n) for the group's agents in `members`: two adjacent
+    // neighbours per lane, 64 per round, one 8-byte load per coordinate when the state is
+    // 8-byte aligned (the pairs start at an even index)
+    auto scan = [&](const int j0, const int n, const unsigned members) {
         auto load2 = [&](int jj, float2 &xv, float2 &yv) {
             if (pl && jj + 1 < n) {
                 xv = __ldg(reinterpret_cast<const float2 *>(a.x + jj));
@@ -725,7 +836,9 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
             load2(jb + 64 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
             const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
             for (int g = 0; g < G; ++g) {   // warp-uniform
-                if (!((members >> g) & 1u)) continue;
+                if constexpr (SEG) {
+                    if (!((members >> g) & 1u)) continue;
+                }
                 const float fx = fd[g].x, fy = fd[g].y;
                 const float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
                 const float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
@@ -747,6 +860,21 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
                 }
             }
         }
+    };
+    if constexpr (SEG) {
+        // one scan per distinct neighbour range (a group may straddle instances)
+        unsigned todo = (1u << G) - 1u;
+        while (todo) {
+            const int gr = __ffs(todo) - 1;
+            const int j0 = s_j0[gr], n = s_j1[gr];
+            unsigned members = 0u;
+            for (int g = 0; g < G; ++g)
+                if (s_j0[g] == j0 && s_j1[g] == n) members |= 1u << g;
+            todo &= ~members;
+            scan(j0, n, members);
+        }
+    } else {
+        scan(cj0, cj1, (1u << G) - 1u);
     }
     if (qn > 0) group_batch<false>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
     if (lane < wqn) {   // the last long or wrapping runs
@@ -980,6 +1108,9 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
     // the double-float sincos table of the update, staged while the pair kernel drains, so
     // that the lookup of the new heading's cos/sin is a shared-memory load
     __shared__ float4 s_sincos[kSinCosTab];
+    // the integral tables (constant inputs) into L2 while the pair kernel still runs
+    prefetch_table_l2(a.g.q, sizeof(longlong2) * (size_t)(a.g.rv + 1));
+    prefetch_table_l2(a.g.cpt, sizeof(longlong2) * (size_t)a.g.rv);
     for (int t = threadIdx.x; t < kSinCosTab; t += blockDim.x) s_sincos[t] = __ldg(a.sctab + t);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, words = a.g.words;
     const int k = blockIdx.x * kFinishWarps + warp;
@@ -1259,8 +1390,10 @@ static int launch_group(StepArgs a, int split, cudaStream_t stream, int *chunks)
     if (c == 1) a.vbits = nullptr;
     *chunks = c;
     const unsigned blocks = (unsigned)groups << shift;
-    return check_cuda(launch_pdl(vpf_pairs_group_kernel, blocks, 32, smem, stream, a),
-                      "vpf_pairs_group_kernel launch");
+    const cudaError_t e =
+        a.seg_begin ? launch_pdl(vpf_pairs_group_seg_kernel<true>, blocks, 32, smem, stream, a)
+                    : launch_pdl(vpf_pairs_group_kernel, blocks, 32, smem, stream, a);
+    return check_cuda(e, "vpf_pairs_group_kernel launch");
 }
 
 template <bool TORUS, bool HETERO, bool TMA>
