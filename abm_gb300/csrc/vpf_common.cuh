@@ -244,6 +244,13 @@ __device__ __forceinline__ ResolveGrid resolve_grid(const GridDev &g) {
 static __device__ __noinline__ int3 resolve_pair(dfl cd, dfl sd, dfl ex, dfl ey, float rj,
                                                  ResolveGrid g, bool unc_t, bool unc_h, float u,
                                                  float ps2, int t, int h) {
+    // the table entries first (predicated loads of clamped indices), so that their latency
+    // overlaps the double-float products below
+    const int kt = min(max((int)floorf(u), 0), max(g.rv - 2, 0));
+    const int kh = (int)rintf(ps2);
+    const int khc = min(max(kh, 0), max(g.kmax - 1, 0));
+    const float4 m = unc_t ? __ldg(g.mid + kt) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 c2 = unc_h ? __ldg(g.cot2 + khc) : make_float2(0.f, 0.f);
     dfl P = df_add(df_mul(cd, ey), df_mul(sd, ex));  // cross(v1, v2) / R
     dfl Q = df_sub(df_mul(cd, ex), df_mul(sd, ey));  // dot(v1, v2) / R
     dfl d2 = df_add(df_mul(ex, ex), df_mul(ey, ey));
@@ -255,23 +262,19 @@ static __device__ __noinline__ int3 resolve_pair(dfl cd, dfl sd, dfl ex, dfl ey,
             t = (df_sign(P) >= 0) ? 0 : g.rv - 1;
             near |= fabsf(P.hi) < 1e-9f * d;
         } else {
-            int k = (int)floorf(u);
-            k = k < 0 ? 0 : (k > g.rv - 2 ? g.rv - 2 : k);
-            float4 m = g.mid[k];
             dfl S = df_add(df_mul(dfl{m.x, m.y}, P), df_mul(dfl{m.z, m.w}, Q));
             // ca > midpoint  <=>  cos(m) P + sin(m) Q < 0; ties go to the lower pixel
-            t = (df_sign(S) < 0) ? k + 1 : k;
+            t = (df_sign(S) < 0) ? kt + 1 : kt;
             near |= fabsf(S.hi) < 1e-9f * d;
         }
     }
     if (unc_h) {
-        int k = (int)rintf(ps2);
+        const int k = kh;
         if (k <= 0) {
             h = 0;
         } else if (k >= g.kmax) {
             h = k - 1;                      // 2 pi k / Rv >= pi/2 > atan(R/d) for d > 0
         } else {
-            float2 c2 = g.cot2[k];
             dfl thr = df_mul(two_prod(rj, rj), dfl{c2.x, c2.y});
             dfl diff = df_sub(thr, d2);     // >= 0  <=>  atan(R/d) >= 2 pi k / Rv
             h = (df_sign(diff) >= 0) ? k : k - 1;
@@ -404,7 +407,7 @@ __device__ __forceinline__ FastEst estimate_fast(const FocalDev &f, float dx, fl
     r.t = (int)ut;
     r.h = (int)hf;
     r.unc = fabsf(fr.x) > 0.5f - g.band_t || fabsf(up.x - g.half_rm1) > g.half_rm1 - g.band_t ||
-            fabsf(fr.y) > 0.5f - g.band_h * fmaxf(up.y, 1.f) || d2 < R2;
+            fabsf(fr.y) > __fmaf_rn(-g.band_h, fmaxf(up.y, 1.f), 0.5f) || d2 < R2;
     return r;
 }
 
