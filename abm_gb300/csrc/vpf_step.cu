@@ -23,6 +23,8 @@
 
 namespace abm {
 
+constexpr int kMaxChunkRounds = 16;
+
 struct StepArgs {
     const float *x, *y, *th, *v;
     float *xo, *yo, *tho, *vo;
@@ -42,6 +44,10 @@ struct StepArgs {
     // into vbits (n x words, zero between steps); NULL for the one-block-per-agent form
     uint32_t *vbits;
     int chunk_shift, chunk_len;
+    // single-swarm group form, round-major chunk plan (chunk_rounds > 0): block b works on
+    // neighbours [chunk_off[r], chunk_off[r + 1]) of group b - r * groups, r = b / groups
+    int chunk_rounds, groups;
+    int chunk_off[kMaxChunkRounds + 1];
     // x and y 8-byte aligned: the l1 form reads two adjacent neighbours per lane (walls, equal
     // radii)
     int pair_loads;
@@ -660,13 +666,21 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     const int words = a.g.words;
     const bool split = a.vbits != nullptr;
     wait_primary_grid();   // the previous step's state (programmatic launch)
-    const int i0 = (int)(blockIdx.x >> a.chunk_shift) * kGroup;
-    const int G = min(kGroup, a.n - i0);
-    int j0 = 0, n = a.n;   // neighbours are [j0, n)
-    if (split) {
-        j0 = (int)(blockIdx.x & ((1u << a.chunk_shift) - 1u)) * a.chunk_len;
-        n = min(n, j0 + a.chunk_len);
+    int grp, j0 = 0, n = a.n;   // neighbours are [j0, n)
+    if (a.chunk_rounds) {   // round-major plan: round r's chunk of every group, r = 0, 1, ...
+        const int r = (int)(blockIdx.x / (unsigned)a.groups);
+        grp = (int)blockIdx.x - r * a.groups;
+        j0 = a.chunk_off[r];
+        n = a.chunk_off[r + 1];
+    } else {
+        grp = (int)(blockIdx.x >> a.chunk_shift);
+        if (split) {
+            j0 = (int)(blockIdx.x & ((1u << a.chunk_shift) - 1u)) * a.chunk_len;
+            n = min(n, j0 + a.chunk_len);
+        }
     }
+    const int i0 = grp * kGroup;
+    const int G = min(kGroup, a.n - i0);
     uint32_t *vball = reinterpret_cast<uint32_t *>(smem);
     size_t off = ((size_t)kGroup * words * 4 + 15) & ~size_t(15);
     FocalDev *fd = reinterpret_cast<FocalDev *>(smem + off);
@@ -1368,18 +1382,42 @@ static int launch_l1(StepArgs a, int wpa, int split, cudaStream_t stream, int *c
     return check_cuda(e, "vpf_pairs_l1_kernel launch");
 }
 
+// Round-major chunk plan of the single-swarm group form with c chunks per group: round r takes
+// a share 2 (c - r) + 1 of every group's neighbours (rounded up to multiples of 64), so the
+// blocks dispatched last are the shortest and the SMs run out of work together.  Measured at
+// N=4096 (8 rounds, 8192 blocks, L2 flushed, three alternating runs): 75.3 us per step with
+// equal chunks in group-major or round-major order, 71.1-71.3 us with decreasing shares (the
+// ramp, and {12,11,10,9,8,6,5,3}/64 or {10,10,10,9,8,7,6,4}/64); 10 rounds 72.1 us, 5 rounds
+// 75.6 us.  Returns the number of rounds and fills off[0..rounds].
+static int chunk_plan(int n, int c, int *off) {
+    c = std::min(c, kMaxChunkRounds);
+    const long long total = (long long)c * c + 2LL * c;   // sum of 2 (c - r) + 1
+    long long acc = 0;
+    int r = 0, at = 0;
+    off[0] = 0;
+    for (int k = 0; k < c && at < n; ++k) {
+        acc += 2LL * (c - k) + 1;
+        int e = k + 1 == c ? n : (int)std::min<long long>(n, (n * acc / total + 63) / 64 * 64);
+        if (e <= at) continue;
+        off[++r] = e;
+        at = e;
+    }
+    return r;
+}
+
 // group form (walls, equal radii, one swarm): chunks as in launch_l1, counted in groups.
 static int launch_group(StepArgs a, int split, cudaStream_t stream, int *chunks) {
     const size_t smem = group_smem_bytes(a.g.words);
     const int groups = (a.n + kGroup - 1) / kGroup;
     int c = 1;
+    long slots = 0;
     if (a.vbits) {
         if (split > 0) {
             c = split;
         } else {
             // about two waves of resident blocks (measured best at N=4096: 8 chunks, 8192
             // blocks; 4 chunks and 16 chunks were 2 us and 4 us slower per step)
-            const long slots = resident_slots((const void *)vpf_pairs_group_kernel, 32, smem);
+            slots = resident_slots((const void *)vpf_pairs_group_kernel, 32, smem);
             while (c < 16 && (long)groups * 2 * c <= 2 * slots && a.n / (2 * c) >= 256) c *= 2;
         }
     }
@@ -1389,7 +1427,17 @@ static int launch_group(StepArgs a, int split, cudaStream_t stream, int *chunks)
     a.chunk_len = c > 1 ? ((a.n + c - 1) / c + 63) / 64 * 64 : a.n;
     if (c == 1) a.vbits = nullptr;
     *chunks = c;
-    const unsigned blocks = (unsigned)groups << shift;
+    unsigned blocks = (unsigned)groups << shift;
+    a.chunk_rounds = 0;
+    // automatic chunks over more than one wave of resident blocks: the decreasing round-major
+    // plan (in a single wave equal chunks are best: the longest block sets the kernel time;
+    // N=1024, 1024 blocks: 37.3 us equal, 40.6 us with the plan)
+    if (c > 1 && split <= 0 && !a.seg_begin && (long)groups * c > slots) {
+        const int rounds = chunk_plan(a.n, c, a.chunk_off);
+        a.chunk_rounds = rounds;
+        a.groups = groups;
+        blocks = (unsigned)groups * (unsigned)rounds;
+    }
     const cudaError_t e =
         a.seg_begin ? launch_pdl(vpf_pairs_group_seg_kernel<true>, blocks, 32, smem, stream, a)
                     : launch_pdl(vpf_pairs_group_kernel, blocks, 32, smem, stream, a);

@@ -1,6 +1,6 @@
 // vpf_tune.cu -- autotuner of the step's launch configuration (abm_vpf_autotune).
 //
-// Every form of the step (group form with 1-16 neighbour chunks, L1 form with 1, 2 or 4 warps
+// Every form of the step (group form with automatic or 1-16 neighbour chunks, L1 form with 1, 2 or 4 warps
 // per focal agent and 1-16 neighbour chunks, tiled form with several agents-per-block and tile
 // lengths) gives bit-identical
 // results, so the best one for a workload is an empirical question: the tuner times each
@@ -21,7 +21,10 @@ static std::vector<abm_step_config> tune_candidates(bool segmented) {
         return c;
     }
     const int chunks[] = {1, 2, 4, 8, 16};
-    for (int ch : chunks) c.push_back({3, 1, ch, 8, 8192, -1.f});   // group form (if it applies)
+    // group form (if it applies): the automatic chunks (with the decreasing round-major plan
+    // beyond one wave of blocks), then 1-16 equal chunks
+    c.push_back({3, 1, 0, 8, 8192, -1.f});
+    for (int ch : chunks) c.push_back({3, 1, ch, 8, 8192, -1.f});
     for (int wpa : wpas)
         for (int ch : chunks) c.push_back({1, wpa, ch, 8, 8192, -1.f});
     const int warps[] = {4, 8, 16};

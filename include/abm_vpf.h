@@ -400,7 +400,10 @@ int abm_vpf_get_step_mode(int32_t *mode, int32_t *warps_per_agent);
  * whose partial bitmasks are OR-ed into a per-agent bitmask in the stream's workspace (Rv/8
  * bytes per agent) and reduced by a second kernel, so that the block scheduler can balance the
  * SMs' work when the swarm alone does not fill the GPU several times over.  0 (the default) =
- * automatic; otherwise 1, 2, 4, 8 or 16.  All values give bit-identical results. */
+ * automatic (in the group form, when the chunks make more than one wave of resident blocks,
+ * the chunks of all groups are dispatched round by round with decreasing lengths, so that the
+ * last blocks are the shortest); otherwise 1, 2, 4, 8 or 16 equal chunks.  All values give
+ * bit-identical results. */
 int abm_vpf_set_step_split(int32_t chunks);
 int abm_vpf_get_step_split(int32_t *chunks);
 
@@ -418,7 +421,8 @@ typedef struct {
  * Autotuner (no counterpart in the reference): times the step on the caller's own state and
  * stream under every candidate configuration and applies the fastest one through
  * abm_vpf_set_step_mode / _config / _split.  Candidates for a single swarm (seg_begin_dev ==
- * NULL): the group form with chunks in {1, 2, 4, 8, 16} (refused where it does not apply), the
+ * NULL): the group form with automatic chunks (chunks = 0) and with chunks in {1, 2, 4, 8, 16}
+ * (refused where it does not apply), the
  * L1 form with warps_per_agent in {1, 2, 4} x chunks in {1, 2, 4, 8, 16}, and the tiled form
  * with warps_per_block in {4, 8, 16} x tile in {1024, 2048, 4096, 8192}; for a
  * batched sweep (segment arrays as for abm_vpf_flock_batched): the group form and the L1 form

@@ -36,7 +36,7 @@ def _current(lib):
 
 
 def test_autotune_single_swarm(restore_config):
-    """27 candidates; the chosen one is the fastest measured and is applied; the step under
+    """33 candidates; the chosen one is the fastest measured and is applied; the step under
     it is bit-identical to the step under the default configuration."""
     from abm_gb300 import _lib, autotune
     from abm_gb300.params import VFParams
@@ -51,7 +51,7 @@ def test_autotune_single_swarm(restore_config):
     s = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
     res = autotune.tune(s, reps=2)
     tried = res["tried"]
-    assert len(tried) == 32   # 5 group-form + 15 L1-form + 12 tiled-form candidates
+    assert len(tried) == 33   # 6 group-form + 15 L1-form + 12 tiled-form candidates
     ran = [t for t in tried if t["ms_per_step"] > 0]
     assert ran, tried
     best = res["best"]

@@ -227,6 +227,18 @@ def test_group_form_partial_last_group():
         _configs_agree(vp, st, ((1, 1, 8, 8192, 1), (3, 1, 8, 8192, 1), (3, 1, 8, 8192, 4)))
 
 
+def test_group_chunk_plan_agrees():
+    """Swarms whose automatic group form spans more than one wave of blocks take the
+    decreasing round-major chunk plan (4096 agents: 8 rounds; 5003 agents: 4 rounds and a last
+    group of 3): bit-identical to the unsplit group form and to the L1 form."""
+    from abm_gb300.params import VFParams
+    for n, W in ((4096, 5000.0), (5003, 5000.0)):
+        st = seeded_swarm(21, n, W, W, R=5.0, kappa=2.0)
+        vp = VFParams(width=W, height=W, rv=3600, radius=5.0)
+        _configs_agree(vp, st, ((0, 1, 8, 8192, 0), (3, 1, 8, 8192, 1), (3, 1, 8, 8192, 4),
+                                (1, 1, 8, 8192, 4)))
+
+
 def test_launch_configs_agree_torus_radii():
     """The same agreement on the infinite (torus) arena with per-agent radii."""
     from abm_gb300.params import VFParams
