@@ -778,6 +778,75 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     if (lane == 0) flush_counters(a, counters);
 }
 
+// Integrals of a batched group's agents at once (the loop form of warp_integrals_loop): lanes
+// 8g .. 8g+7 take agent g's words w = lane & 7, w + 8, ..., each visiting its words' transitions,
+// and a reduction over the agent's 8 lanes gives its sums (exact fixed point, so the same sums
+// as one agent at a time over 32 lanes).  agents: the group's agent ids; also copies each
+// agent's bitmask to a.bits when requested.
+__device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *agents, int G,
+                                                  const uint32_t *vball) {
+    const int lane = threadIdx.x & 31;
+    const int g = lane >> 3, sub = lane & 7;
+    const int rv = a.g.rv, words = a.g.words;
+    const bool act = g < G;
+    const uint32_t *vb = vball + (act ? g : 0) * words;
+    const uint32_t v0 = vb[0] & 1u;
+    const uint32_t vl = (vb[(rv - 1) >> 5] >> ((rv - 1) & 31)) & 1u;
+    const int bwd = (v0 == 1u && vl == 0u) ? 1 : 0;
+    long long bc = 0, bs = 0, ec = 0, es = 0;
+    if (act) {
+        for (int w = sub; w < words; w += 8) {
+            const uint32_t cur = vb[w];
+            const uint32_t prev = (w > 0) ? (vb[w - 1] >> 31) : (cur & 1u);
+            uint32_t D = cur ^ ((cur << 1) | prev);
+            if (w == words - 1 && (rv & 31)) D &= (1u << (rv & 31)) - 1u;
+            while (D) {
+                const int b = __ffs(D) - 1;
+                D &= D - 1u;
+                const int j = (w << 5) + b;
+                const longlong2 qv = a.g.q[j];
+                if ((cur >> b) & 1u) {   // run starts at j
+                    bc -= qv.x;
+                    bs -= qv.y;
+                } else {                 // run ends at j
+                    bc += qv.x;
+                    bs += qv.y;
+                }
+                const longlong2 cv = a.g.cpt[j - 1 + bwd];
+                ec += cv.x;
+                es += cv.y;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {   // within each agent's 8 lanes
+        bc += __shfl_xor_sync(ABM_FULL_MASK, bc, o);
+        bs += __shfl_xor_sync(ABM_FULL_MASK, bs, o);
+        ec += __shfl_xor_sync(ABM_FULL_MASK, ec, o);
+        es += __shfl_xor_sync(ABM_FULL_MASK, es, o);
+    }
+    if (!act) return;
+    const int i = agents[g];
+    if (sub == 0) {
+        if (vl) {
+            bc += a.g.qc_total;
+            bs += a.g.qs_total;
+        }
+        if (v0 != vl) {   // the circular edge between pixels Rv-1 and 0
+            const longlong2 cv = a.g.cpt[bwd ? 0 : rv - 1];
+            ec += cv.x;
+            es += cv.y;
+        }
+        longlong2 *sp = reinterpret_cast<longlong2 *>(a.sums) + 2 * (size_t)i;
+        sp[0] = make_longlong2(bc, bs);
+        sp[1] = make_longlong2(ec, es);
+    }
+    if (a.bits) {
+        uint32_t *dst = a.bits + (size_t)i * words;
+        for (int w = sub; w < words; w += 8) dst[w] = vb[w];
+    }
+}
+
 // The group form for a batched sweep: the group is 4 consecutive entries of the schedule, and
 // each distinct neighbour range of its agents (a group may straddle instances) is scanned once
 // for the agents that share it.  (A separate kernel: folding this into the single-swarm kernel
@@ -918,9 +987,7 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_seg_kernel(const StepArgs 
             if (v) atomicOr(gb + w, v);
         }
     } else {       // integrals of each agent (the drained queues hold its transition list)
-        for (int g = 0; g < G; ++g)
-            finish_agent(a, s_agent[g], vball + g * words, reinterpret_cast<uint32_t *>(q),
-                         kListCap<false>);
+        group_finish_loop(a, s_agent, G, vball);
     }
     if (lane == 0) flush_counters(a, counters);
 }
