@@ -596,70 +596,103 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
 constexpr int kGroup = 4;
 constexpr int kGroupTagShift = 24;   // neighbour indices below 2^24
 
+constexpr int kCounters = 4;   // a group block's counters, then 33 spare words (lane, lane + 1)
+
+// Shared memory of a group block: the agents' bitmasks (the second OR of a short run may name
+// the word after the last agent's bitmask: the padding or the focal records, which an OR of
+// zero leaves unchanged), the focal records, the queues, the counters and the spare words.
 static size_t group_smem_bytes(int words) {
     size_t b = ((size_t)kGroup * words * sizeof(uint32_t) + 15) & ~size_t(15);
     b += ((size_t)kGroup * sizeof(FocalDev) + 15) & ~size_t(15);
     b += (size_t)(kQueue + kQueue2) * sizeof(QEntry<false>) + kQueueW * sizeof(int2);
-    return b + 16;
+    return b + (kCounters + 33) * sizeof(unsigned);
 }
 
-// Phase B of up to 32 queued (agent slot, neighbour) candidates (lane < cnt holds one).
-template <bool FULL>
-__device__ __forceinline__ void group_batch(const FocalDev *fd, const QEntry<false> *q, int cnt,
-                                            QEntry<false> *q2, int &q2n, int2 *wq, int &wqn,
-                                            uint32_t *vball, const StepArgs &a,
-                                            unsigned *counters) {
+// Phase B of one (agent slot, neighbour) candidate per lane (`have`: the lane holds one; e: its
+// offset, d^2 and tagged neighbour index): FP32 decisions, rasterisation of short runs, long and
+// wrapping runs to the run queue, guard-band pairs to the double-float queue (each drained 32
+// at a time).  FULLFOV: the field of view is the whole circle, so every projection is visible.
+template <bool FULLFOV>
+__device__ __forceinline__ void group_candidate(const FocalDev *fd, const QEntry<false> &e,
+                                                bool have, QEntry<false> *q2, int &q2n, int2 *wq,
+                                                int &wqn, uint32_t *vball, const StepArgs &a,
+                                                unsigned *counters) {
     const int lane = threadIdx.x & 31;
     const int words = a.g.words;
-    const bool have = FULL || lane < cnt;
-    const QEntry<false> e = (FULL || have) ? q[lane] : QEntry<false>::make(1.f, 0.f, 1.f, 0);
     const int g = (int)((unsigned)e.j() >> kGroupTagShift);
     const FastEst est = estimate_fast(fd[g], e.v.x, e.v.y, e.v.z, a.radius0,
                                       a.radius0 * a.radius0, a.g);
     const bool unc = have && est.unc;
     const int s = est.t - est.h, en = est.t + est.h;
-    const bool vis = have && !est.unc && (a.g.full_fov || projection_visible(a.g, s, en));
+    const bool vis = have && !est.unc && (FULLFOV || projection_visible(a.g, s, en));
     const unsigned len = (unsigned)(en - s);
     const bool short_run = s >= 0 && en < a.g.rv && len <= 32u;
-    if (vis && short_run) raster_short(vball + g * words, s, len);
+    {   // short runs: two shared ORs on every lane, without a branch (lanes with nothing to
+        // raster OR zero into their own spare words after the block's counters; measured 3 %
+        // faster steps than predicated ORs)
+        const bool rs = vis && short_run;
+        uint32_t *vb = rs ? vball + g * words + (s >> 5) : counters + kCounters + lane;
+        const uint32_t m = rs ? __funnelshift_rc(ABM_FULL_MASK, 0u, 32u - len) : 0u;
+        const int sh = s & 31;
+        atomicOr(vb, m << sh);
+        atomicOr(vb + 1, __funnelshift_l(m, 0u, sh));   // may name the next agent's word 0
+    }
     const unsigned lt = (1u << lane) - 1u;
-    const unsigned wm = __ballot_sync(ABM_FULL_MASK, vis && !short_run);
-    if (wm) {   // long and wrapping runs wait in the run queue (slot in the top byte of e)
-        if (vis && !short_run) wq[wqn + __popc(wm & lt)] = make_int2(s, en | (g << kGroupTagShift));
-        wqn += __popc(wm);
+    // one vote for the rare cases: a long or wrapping run, or a guard-band decision
+    const bool lng = vis && !short_run;
+    if (__ballot_sync(ABM_FULL_MASK, lng || unc)) {
+        const unsigned wm = __ballot_sync(ABM_FULL_MASK, lng);
+        if (wm) {   // long and wrapping runs wait in the run queue (slot in the top byte)
+            if (lng) wq[wqn + __popc(wm & lt)] = make_int2(s, en | (g << kGroupTagShift));
+            wqn += __popc(wm);
+            __syncwarp();
+            if (wqn >= 32) {
+                wqn -= 32;
+                const int2 r = wq[wqn + lane];
+                raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
+                                  r.y & ((1 << kGroupTagShift) - 1));
+                __syncwarp();
+            }
+        }
+        const unsigned um = __ballot_sync(ABM_FULL_MASK, unc);
+        if (um) {   // defer the uncertain ones to the double-float queue
+            if (unc) q2[q2n + __popc(um & lt)] = e;
+            q2n += __popc(um);
+        }
         __syncwarp();
-        if (wqn >= 32) {
-            wqn -= 32;
-            const int2 r = wq[wqn + lane];
-            raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
-                              r.y & ((1 << kGroupTagShift) - 1));
+        if (q2n >= 32) {   // drain 32 deferred pairs (warp-uniform)
+            q2n -= 32;
+            const int tag = q2[q2n + lane].j();
+            const int dg = (int)((unsigned)tag >> kGroupTagShift);
+            const int j = tag & ((1 << kGroupTagShift) - 1);
+            const bool near = resolve_and_raster<false, false>(fd[dg], __ldg(a.x + j),
+                                                               __ldg(a.y + j), a.radius0,
+                                                               vball + dg * words, a);
+            const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
+            if (lane == 0) {
+                atomicAdd(&counters[0], 32u);
+                if (nm) atomicAdd(&counters[1], (unsigned)__popc(nm));
+            }
             __syncwarp();
         }
     }
-    const unsigned um = __ballot_sync(ABM_FULL_MASK, unc);
-    if (um) {   // defer the uncertain ones to the double-float queue
-        if (unc) q2[q2n + __popc(um & lt)] = e;
-        q2n += __popc(um);
-    }
-    __syncwarp();
-    if (q2n >= 32) {   // drain 32 deferred pairs (warp-uniform)
-        q2n -= 32;
-        const int tag = q2[q2n + lane].j();
-        const int dg = (int)((unsigned)tag >> kGroupTagShift);
-        const int j = tag & ((1 << kGroupTagShift) - 1);
-        const bool near = resolve_and_raster<false, false>(fd[dg], __ldg(a.x + j), __ldg(a.y + j),
-                                                           a.radius0, vball + dg * words, a);
-        const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
-        if (lane == 0) {
-            atomicAdd(&counters[0], 32u);
-            if (nm) atomicAdd(&counters[1], (unsigned)__popc(nm));
-        }
-        __syncwarp();
-    }
+}
+
+// Phase B of up to 32 queued candidates (lane < cnt holds one).
+template <bool FULL, bool FULLFOV>
+__device__ __forceinline__ void group_batch(const FocalDev *fd, const QEntry<false> *q, int cnt,
+                                            QEntry<false> *q2, int &q2n, int2 *wq, int &wqn,
+                                            uint32_t *vball, const StepArgs &a,
+                                            unsigned *counters) {
+    const int lane = threadIdx.x & 31;
+    const bool have = FULL || lane < cnt;
+    const QEntry<false> e = (FULL || have) ? q[lane] : QEntry<false>::make(1.f, 0.f, 1.f, 0);
+    group_candidate<FULLFOV>(fd, e, have, q2, q2n, wq, wqn, vball, a, counters);
 }
 
 // The group form for one swarm: the group is 4 consecutive agents, the neighbours the block's
 // chunk.
+template <bool FULLFOV>
 __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x;
@@ -739,11 +772,11 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
             __syncwarp();
             while (qn >= 32) {   // warp-uniform; at most two batches
                 qn -= 32;
-                group_batch<true>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a, counters);
+                group_batch<true, FULLFOV>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a, counters);
             }
         }
     }
-    if (qn > 0) group_batch<false>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
+    if (qn > 0) group_batch<false, FULLFOV>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
     if (lane < wqn) {   // the last long or wrapping runs
         const int2 r = wq[lane];
         raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
@@ -850,24 +883,19 @@ __device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *
 // The group form for a batched sweep: the group is 4 consecutive entries of the schedule, and
 // each distinct neighbour range of its agents (a group may straddle instances) is scanned once
 // for the agents that share it.  (A separate kernel: folding this into the single-swarm kernel
-// measured 1.3 us slower per step at N=4096.)
-template <bool SEG>
+// measured 1.3 us slower per step at N=4096.)  DIRECT: the arena lies within the cull radius,
+// so (almost) every pair is live and phase B takes the candidates straight from the scan,
+// without the queue that compacts the live ones.
+template <bool FULLFOV, bool DIRECT>
 __global__ void __launch_bounds__(32) vpf_pairs_group_seg_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_agent[kGroup], s_j0[kGroup], s_j1[kGroup];
     const int lane = threadIdx.x;
     const int words = a.g.words;
-    const bool split = a.vbits != nullptr;
     wait_primary_grid();   // the previous step's state (programmatic launch)
-    // the group: positions [p0, p0 + G) of the agent order (a batched sweep's schedule, else
-    // the agents themselves); neighbours of a single swarm: the block's chunk
-    const int p0 = (int)(blockIdx.x >> a.chunk_shift) * kGroup;
+    // the group: positions [p0, p0 + G) of the schedule
+    const int p0 = (int)blockIdx.x * kGroup;
     const int G = min(kGroup, a.n - p0);
-    int cj0 = 0, cj1 = a.n;
-    if (split) {
-        cj0 = (int)(blockIdx.x & ((1u << a.chunk_shift) - 1u)) * a.chunk_len;
-        cj1 = min(cj1, cj0 + a.chunk_len);
-    }
     uint32_t *vball = reinterpret_cast<uint32_t *>(smem);
     size_t off = ((size_t)kGroup * words * 4 + 15) & ~size_t(15);
     FocalDev *fd = reinterpret_cast<FocalDev *>(smem + off);
@@ -883,10 +911,10 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_seg_kernel(const StepArgs 
     if (lane < 4) counters[lane] = 0u;
     allow_dependent_launch();
     if (lane < G) {   // the group's agents at once
-        const int i = (SEG && a.order) ? a.order[p0 + lane] : p0 + lane;
+        const int i = a.order ? a.order[p0 + lane] : p0 + lane;
         s_agent[lane] = i;
-        s_j0[lane] = SEG ? a.seg_begin[i] : cj0;
-        s_j1[lane] = SEG ? a.seg_end[i] : cj1;
+        s_j0[lane] = a.seg_begin[i];
+        s_j1[lane] = a.seg_end[i];
         fd[lane] = load_focal<false>(a, i);
     }
     __syncwarp();
@@ -895,8 +923,6 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_seg_kernel(const StepArgs 
     int qn = 0, q2n = 0, wqn = 0;
     const unsigned lt = (1u << lane) - 1u;
     const bool pl = a.pair_loads != 0;
-    // one scan per distinct neighbour range of the group's agents (one for a single swarm; a
-    // group may straddle instances of a batched sweep)
     // one scan of a neighbour range [j0, n) for the group's agents in `members`: two adjacent
     // neighbours per lane, 64 per round, one 8-byte load per coordinate when the state is
     // 8-byte aligned (the pairs start at an even index)
@@ -919,47 +945,51 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_seg_kernel(const StepArgs 
             load2(jb + 64 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
             const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
             for (int g = 0; g < G; ++g) {   // warp-uniform
-                if constexpr (SEG) {
-                    if (!((members >> g) & 1u)) continue;
-                }
+                if (!((members >> g) & 1u)) continue;
                 const float fx = fd[g].x, fy = fd[g].y;
                 const float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
                 const float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
                 const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
                 const bool live0 = v0 && d2.x > 0.f && d2.x <= cull_r2;
                 const bool live1 = v1 && d2.y > 0.f && d2.y <= cull_r2;
-                const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
-                const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
-                const int c0 = __popc(lm0);
                 const int tag = jj | (g << kGroupTagShift);
-                if (live0) q[qn + __popc(lm0 & lt)] = QEntry<false>::make(dx.x, dy.x, d2.x, tag);
-                if (live1)
-                    q[qn + c0 + __popc(lm1 & lt)] = QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1);
-                qn += c0 + __popc(lm1);
-                __syncwarp();
-                while (qn >= 32) {   // warp-uniform; at most two batches
-                    qn -= 32;
-                    group_batch<true>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a, counters);
+                if constexpr (DIRECT) {   // phase B on the lanes' own candidates
+                    group_candidate<FULLFOV>(fd, QEntry<false>::make(dx.x, dy.x, d2.x, tag),
+                                             live0, q2, q2n, wq, wqn, vball, a, counters);
+                    group_candidate<FULLFOV>(fd, QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1),
+                                             live1, q2, q2n, wq, wqn, vball, a, counters);
+                } else {
+                    const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
+                    const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
+                    const int c0 = __popc(lm0);
+                    if (live0)
+                        q[qn + __popc(lm0 & lt)] = QEntry<false>::make(dx.x, dy.x, d2.x, tag);
+                    if (live1)
+                        q[qn + c0 + __popc(lm1 & lt)] =
+                            QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1);
+                    qn += c0 + __popc(lm1);
+                    __syncwarp();
+                    while (qn >= 32) {   // warp-uniform; at most two batches
+                        qn -= 32;
+                        group_batch<true, FULLFOV>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a,
+                                                   counters);
+                    }
                 }
             }
         }
     };
-    if constexpr (SEG) {
-        // one scan per distinct neighbour range (a group may straddle instances)
-        unsigned todo = (1u << G) - 1u;
-        while (todo) {
-            const int gr = __ffs(todo) - 1;
-            const int j0 = s_j0[gr], n = s_j1[gr];
-            unsigned members = 0u;
-            for (int g = 0; g < G; ++g)
-                if (s_j0[g] == j0 && s_j1[g] == n) members |= 1u << g;
-            todo &= ~members;
-            scan(j0, n, members);
-        }
-    } else {
-        scan(cj0, cj1, (1u << G) - 1u);
+    // one scan per distinct neighbour range (a group may straddle instances)
+    unsigned todo = (1u << G) - 1u;
+    while (todo) {
+        const int gr = __ffs(todo) - 1;
+        const int j0 = s_j0[gr], n = s_j1[gr];
+        unsigned members = 0u;
+        for (int g = 0; g < G; ++g)
+            if (s_j0[g] == j0 && s_j1[g] == n) members |= 1u << g;
+        todo &= ~members;
+        scan(j0, n, members);
     }
-    if (qn > 0) group_batch<false>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
+    if (qn > 0) group_batch<false, FULLFOV>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
     if (lane < wqn) {   // the last long or wrapping runs
         const int2 r = wq[lane];
         raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
@@ -980,15 +1010,8 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_seg_kernel(const StepArgs 
         counters[1] += (unsigned)__popc(nm);
     }
     __syncwarp();
-    if (split) {   // the group's partial bitmasks (consecutive agents) into the workspace
-        uint32_t *gb = a.vbits + (size_t)p0 * words;
-        for (int w = lane; w < G * words; w += 32) {
-            const uint32_t v = vball[w];
-            if (v) atomicOr(gb + w, v);
-        }
-    } else {       // integrals of each agent (the drained queues hold its transition list)
-        group_finish_loop(a, s_agent, G, vball);
-    }
+    // integrals of each agent (the whole neighbour ranges were scanned)
+    group_finish_loop(a, s_agent, G, vball);
     if (lane == 0) flush_counters(a, counters);
 }
 
@@ -1473,7 +1496,8 @@ static int chunk_plan(int n, int c, int *off) {
 }
 
 // group form (walls, equal radii, one swarm): chunks as in launch_l1, counted in groups.
-static int launch_group(StepArgs a, int split, cudaStream_t stream, int *chunks) {
+static int launch_group(StepArgs a, int split, double arena_w, double arena_h,
+                        cudaStream_t stream, int *chunks) {
     const size_t smem = group_smem_bytes(a.g.words);
     const int groups = (a.n + kGroup - 1) / kGroup;
     int c = 1;
@@ -1484,7 +1508,7 @@ static int launch_group(StepArgs a, int split, cudaStream_t stream, int *chunks)
         } else {
             // about two waves of resident blocks (measured best at N=4096: 8 chunks, 8192
             // blocks; 4 chunks and 16 chunks were 2 us and 4 us slower per step)
-            slots = resident_slots((const void *)vpf_pairs_group_kernel, 32, smem);
+            slots = resident_slots((const void *)vpf_pairs_group_kernel<true>, 32, smem);
             while (c < 16 && (long)groups * 2 * c <= 2 * slots && a.n / (2 * c) >= 256) c *= 2;
         }
     }
@@ -1505,9 +1529,21 @@ static int launch_group(StepArgs a, int split, cudaStream_t stream, int *chunks)
         a.groups = groups;
         blocks = (unsigned)groups * (unsigned)rounds;
     }
-    const cudaError_t e =
-        a.seg_begin ? launch_pdl(vpf_pairs_group_seg_kernel<true>, blocks, 32, smem, stream, a)
-                    : launch_pdl(vpf_pairs_group_kernel, blocks, 32, smem, stream, a);
+    const bool ff = a.g.full_fov != 0;
+    cudaError_t e;
+    if (a.seg_begin) {
+        // direct phase B when the whole arena lies within the cull radius (then every pair of
+        // agents inside it is live); any state is still handled exactly, only more slowly
+        const double ext2 = (double)arena_w * arena_w + (double)arena_h * arena_h;
+        const bool direct = ext2 <= (double)a.radius0 * a.radius0 * a.g.cull;
+        if (ff && direct) e = launch_pdl(vpf_pairs_group_seg_kernel<true, true>, blocks, 32, smem, stream, a);
+        else if (ff) e = launch_pdl(vpf_pairs_group_seg_kernel<true, false>, blocks, 32, smem, stream, a);
+        else if (direct) e = launch_pdl(vpf_pairs_group_seg_kernel<false, true>, blocks, 32, smem, stream, a);
+        else e = launch_pdl(vpf_pairs_group_seg_kernel<false, false>, blocks, 32, smem, stream, a);
+    } else {
+        e = ff ? launch_pdl(vpf_pairs_group_kernel<true>, blocks, 32, smem, stream, a)
+               : launch_pdl(vpf_pairs_group_kernel<false>, blocks, 32, smem, stream, a);
+    }
     return check_cuda(e, "vpf_pairs_group_kernel launch");
 }
 
@@ -1862,7 +1898,7 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     const bool use_l1 = !use_group && (seg_begin || mode == 1 || (mode == 0 && n <= 16384));
     int chunks = 1;
     if (use_group) {
-        st = launch_group(a, split, s, &chunks);
+        st = launch_group(a, split, p->width, p->height, s, &chunks);
     } else if (use_l1) {
         if (!torus && !hetero) st = launch_l1<false, false>(a, wpa, split, s, &chunks);
         else if (!torus && hetero) st = launch_l1<false, true>(a, wpa, split, s, &chunks);
