@@ -595,15 +595,18 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
 // exactly as in the l1 form and the group's partial bitmasks are OR-ed into the workspace.
 constexpr int kGroup = 4;
 constexpr int kGroupTagShift = 24;   // neighbour indices below 2^24
+// batched sweeps: groups of 8 schedule entries (512-instance sweep step 256.0 -> 239.6 us
+// against groups of 4: the per-block costs are shared by twice the agents)
+constexpr int kSegGroup = 8;
 
 constexpr int kCounters = 4;   // a group block's counters, then 33 spare words (lane, lane + 1)
 
 // Shared memory of a group block: the agents' bitmasks (the second OR of a short run may name
 // the word after the last agent's bitmask: the padding or the focal records, which an OR of
 // zero leaves unchanged), the focal records, the queues, the counters and the spare words.
-static size_t group_smem_bytes(int words) {
-    size_t b = ((size_t)kGroup * words * sizeof(uint32_t) + 15) & ~size_t(15);
-    b += ((size_t)kGroup * sizeof(FocalDev) + 15) & ~size_t(15);
+static size_t group_smem_bytes(int words, int gs = kGroup) {
+    size_t b = ((size_t)gs * words * sizeof(uint32_t) + 15) & ~size_t(15);
+    b += ((size_t)gs * sizeof(FocalDev) + 15) & ~size_t(15);
     b += (size_t)(kQueue + kQueue2) * sizeof(QEntry<false>) + kQueueW * sizeof(int2);
     return b + (kCounters + 33) * sizeof(unsigned);
 }
@@ -811,15 +814,16 @@ __global__ void __launch_bounds__(32) vpf_pairs_group_kernel(const StepArgs a) {
     if (lane == 0) flush_counters(a, counters);
 }
 
-// Integrals of a batched group's agents at once (the loop form of warp_integrals_loop): lanes
-// 8g .. 8g+7 take agent g's words w = lane & 7, w + 8, ..., each visiting its words' transitions,
-// and a reduction over the agent's 8 lanes gives its sums (exact fixed point, so the same sums
-// as one agent at a time over 32 lanes).  agents: the group's agent ids; also copies each
+// Integrals of a batched group's agents at once (the loop form of warp_integrals_loop): the
+// LPA = 32 / kSegGroup lanes LPA g .. LPA g + LPA - 1 take agent g's words w = lane % LPA,
+// w + LPA, ..., each visiting its words' transitions, and a reduction over the agent's lanes
+// gives its sums (exact fixed point, so the same sums as one agent at a time over 32 lanes).  agents: the group's agent ids; also copies each
 // agent's bitmask to a.bits when requested.
 __device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *agents, int G,
                                                   const uint32_t *vball) {
     const int lane = threadIdx.x & 31;
-    const int g = lane >> 3, sub = lane & 7;
+    constexpr int LPA = 32 / kSegGroup;
+    const int g = lane / LPA, sub = lane % LPA;
     const int rv = a.g.rv, words = a.g.words;
     const bool act = g < G;
     const uint32_t *vb = vball + (act ? g : 0) * words;
@@ -828,7 +832,7 @@ __device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *
     const int bwd = (v0 == 1u && vl == 0u) ? 1 : 0;
     long long bc = 0, bs = 0, ec = 0, es = 0;
     if (act) {
-        for (int w = sub; w < words; w += 8) {
+        for (int w = sub; w < words; w += LPA) {
             const uint32_t cur = vb[w];
             const uint32_t prev = (w > 0) ? (vb[w - 1] >> 31) : (cur & 1u);
             uint32_t D = cur ^ ((cur << 1) | prev);
@@ -852,7 +856,7 @@ __device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *
         }
     }
 #pragma unroll
-    for (int o = 4; o > 0; o >>= 1) {   // within each agent's 8 lanes
+    for (int o = LPA / 2; o > 0; o >>= 1) {   // within each agent's lanes
         bc += __shfl_xor_sync(ABM_FULL_MASK, bc, o);
         bs += __shfl_xor_sync(ABM_FULL_MASK, bs, o);
         ec += __shfl_xor_sync(ABM_FULL_MASK, ec, o);
@@ -876,30 +880,31 @@ __device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *
     }
     if (a.bits) {
         uint32_t *dst = a.bits + (size_t)i * words;
-        for (int w = sub; w < words; w += 8) dst[w] = vb[w];
+        for (int w = sub; w < words; w += LPA) dst[w] = vb[w];
     }
 }
 
-// The group form for a batched sweep: the group is 4 consecutive entries of the schedule, and
-// each distinct neighbour range of its agents (a group may straddle instances) is scanned once
-// for the agents that share it.  (A separate kernel: folding this into the single-swarm kernel
-// measured 1.3 us slower per step at N=4096.)  DIRECT: the arena lies within the cull radius,
+// The group form for a batched sweep: the group is kSegGroup consecutive entries of the
+// schedule, and each distinct neighbour range of its agents (a group may straddle instances)
+// is scanned once for the agents that share it.  (A separate kernel: folding this into the
+// single-swarm kernel measured 1.3 us slower per step at N=4096.)  DIRECT: the arena lies
+// within the cull radius,
 // so (almost) every pair is live and phase B takes the candidates straight from the scan,
 // without the queue that compacts the live ones.
 template <bool FULLFOV, bool DIRECT>
 __global__ void __launch_bounds__(32) vpf_pairs_group_seg_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int s_agent[kGroup], s_j0[kGroup], s_j1[kGroup];
+    __shared__ int s_agent[kSegGroup], s_j0[kSegGroup], s_j1[kSegGroup];
     const int lane = threadIdx.x;
     const int words = a.g.words;
     wait_primary_grid();   // the previous step's state (programmatic launch)
     // the group: positions [p0, p0 + G) of the schedule
-    const int p0 = (int)blockIdx.x * kGroup;
-    const int G = min(kGroup, a.n - p0);
+    const int p0 = (int)blockIdx.x * kSegGroup;
+    const int G = min(kSegGroup, a.n - p0);
     uint32_t *vball = reinterpret_cast<uint32_t *>(smem);
-    size_t off = ((size_t)kGroup * words * 4 + 15) & ~size_t(15);
+    size_t off = ((size_t)kSegGroup * words * 4 + 15) & ~size_t(15);
     FocalDev *fd = reinterpret_cast<FocalDev *>(smem + off);
-    off += ((size_t)kGroup * sizeof(FocalDev) + 15) & ~size_t(15);
+    off += ((size_t)kSegGroup * sizeof(FocalDev) + 15) & ~size_t(15);
     QEntry<false> *q = reinterpret_cast<QEntry<false> *>(smem + off);
     QEntry<false> *q2 = q + kQueue;
     off += (size_t)(kQueue + kQueue2) * sizeof(QEntry<false>);
@@ -1209,13 +1214,12 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
     extern __shared__ __align__(16) unsigned char fsmem[];
     __shared__ longlong2 sums[kFinishWarps][2];
     __shared__ FinishInputs uin[kFinishWarps];
-    // the double-float sincos table of the update, staged while the pair kernel drains, so
-    // that the lookup of the new heading's cos/sin is a shared-memory load
-    __shared__ float4 s_sincos[kSinCosTab];
-    // the integral tables (constant inputs) into L2 while the pair kernel still runs
+    // the integral tables and the update's double-float sincos table (constant inputs) into
+    // L2 while the pair kernel still runs (staging the sincos table in shared memory in every
+    // block measured 0.4 us slower per step at N=4096)
     prefetch_table_l2(a.g.q, sizeof(longlong2) * (size_t)(a.g.rv + 1));
     prefetch_table_l2(a.g.cpt, sizeof(longlong2) * (size_t)a.g.rv);
-    for (int t = threadIdx.x; t < kSinCosTab; t += blockDim.x) s_sincos[t] = __ldg(a.sctab + t);
+    prefetch_table_l2(a.sctab, sizeof(float4) * kSinCosTab);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, words = a.g.words;
     const int k = blockIdx.x * kFinishWarps + warp;
     const int ku = blockIdx.x * kFinishWarps + lane;
@@ -1276,7 +1280,7 @@ __global__ void __launch_bounds__(32 * kFinishWarps) vpf_finish_kernel(const Ste
     const dfl alp0 = a.alp0 ? dfl{in.alp0, 0.f} : a.ud.alp0;
     const dfl bet0 = a.bet0 ? dfl{in.bet0, 0.f} : a.ud.bet0;
     const dfl v0 = a.v0 ? dfl{in.v0, 0.f} : a.ud.v0;
-    const UpdateOut o = update_agent_df(a.ud, s_sincos, in.x, in.y, in.th, in.v, in.R, s0.x,
+    const UpdateOut o = update_agent_df(a.ud, a.sctab, in.x, in.y, in.th, in.v, in.R, s0.x,
                                         s0.y, s1.x, s1.y, alp0, bet0, v0);
     store_update(a, ku, o);
 }
@@ -1498,8 +1502,9 @@ static int chunk_plan(int n, int c, int *off) {
 // group form (walls, equal radii, one swarm): chunks as in launch_l1, counted in groups.
 static int launch_group(StepArgs a, int split, double arena_w, double arena_h,
                         cudaStream_t stream, int *chunks) {
-    const size_t smem = group_smem_bytes(a.g.words);
-    const int groups = (a.n + kGroup - 1) / kGroup;
+    const int gsz = a.seg_begin ? kSegGroup : kGroup;
+    const size_t smem = group_smem_bytes(a.g.words, gsz);
+    const int groups = (a.n + gsz - 1) / gsz;
     int c = 1;
     long slots = 0;
     if (a.vbits) {

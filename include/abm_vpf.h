@@ -280,8 +280,9 @@ int abm_vpf_flock_run_recorded(abm_swarm_state *a, abm_swarm_state *b, int32_t n
  * per-agent VSWRM sums between the two launches, the lookup tables of one grid and the
  * double-float sincos table) lives in a file-scope device array of about 2.5 MiB that every GPU
  * loading the library holds until the process exits; no cudaMalloc, cudaFree or other
- * allocating routine is called.  Up to 16384 agents it runs the one-block-per-agent pair
- * kernel, above that the tiled one (neither needs the bitmask workspace of the split form).
+ * allocating routine is called.  Up to 16384 agents it runs the group pair kernel without
+ * neighbour chunks (walls, equal radii) or the one-block-per-agent one, above that the tiled
+ * one (none of them needs the bitmask workspace of the split form).
  * Limits: n <= ABM_NOALLOC_MAX_AGENTS and rv <= ABM_NOALLOC_MAX_RV, larger values return
  * ABM_ERR_INVALID_ARG / ABM_ERR_RV with a message.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) and copies the sincos table into it, and a call
