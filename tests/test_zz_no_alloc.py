@@ -5,9 +5,10 @@ memory pool, a process that reserved all device memory); the no-alloc entry poin
 from a fixed file-scope scratch array.  This test calls both entry points through the C ABI on
 calls in a row, with different swarm sizes and grids so each call has to replace the array's
 previous contents, and checks that the results agree within the parity tolerances the other GPU
-tests use (they are in fact expected to be bit-identical).  The sizes cover both pair kernels
-the entry point uses: the one-block-per-agent form (up to 16384 agents) and the tiled form
-(above).  It also checks the size limits.  The file name makes pytest collect it last.
+tests use (they are in fact expected to be bit-identical).  The cases cover the three pair
+kernels the entry point uses: up to 16384 agents the group form without neighbour chunks (walls,
+equal radii) and the one-block-per-agent form (the torus), above that the tiled form.  It also
+checks the size limits.  The file name makes pytest collect it last.
 """
 import ctypes
 
