@@ -847,8 +847,8 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_kernel(const StepArgs 
 // Integrals of a batched group's agents at once (the loop form of warp_integrals_loop): the
 // LPA = 32 / kSegGroup lanes LPA g .. LPA g + LPA - 1 take agent g's words w = lane % LPA,
 // w + LPA, ..., each visiting its words' transitions, and a reduction over the agent's lanes
-// gives its sums (exact fixed point, so the same sums as one agent at a time over 32 lanes).  agents: the group's agent ids; also copies each
-// agent's bitmask to a.bits when requested.
+// gives its sums (exact fixed point, so the same sums as one agent at a time over 32 lanes).
+// agents: the group's agent ids; also copies each agent's bitmask to a.bits when requested.
 __device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *agents, int G,
                                                   const uint32_t *vball) {
     const int lane = threadIdx.x & 31;
@@ -918,9 +918,8 @@ __device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *
 // schedule, and each distinct neighbour range of its agents (a group may straddle instances)
 // is scanned once for the agents that share it.  (A separate kernel: folding this into the
 // single-swarm kernel measured 1.3 us slower per step at N=4096.)  DIRECT: the arena lies
-// within the cull radius,
-// so (almost) every pair is live and phase B takes the candidates straight from the scan,
-// without the queue that compacts the live ones.
+// within the cull radius, so (almost) every pair is live and phase B takes the candidates
+// straight from the scan, without the queue that compacts the live ones.
 template <bool FULLFOV, bool DIRECT>
 __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
