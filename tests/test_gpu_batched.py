@@ -180,3 +180,37 @@ def test_polarisation_statistic_on_device():
     assert np.max(np.abs(pa - np.array(want).T)) < 1e-6
     b.run(120, chunk=100)
     assert np.array_equal(b.polarisation(), pa)
+
+
+@pytest.mark.parametrize("width,fov", [(600.0, None), (600.0, (-1.5, 2.0)), (3000.0, None),
+                                       (3000.0, (-1.5, 2.0))])
+def test_batched_group_kernel_forms_agree(width, fov):
+    """The batched group kernel's four forms -- phase B straight from the scan (an arena
+    inside the cull radius) or through the compaction queue (a larger arena), each with the
+    full field of view or a partial one -- against the L1 form on the same sweep: VPF, terms
+    and new state bit-identical."""
+    import math
+    from abm_gb300 import _lib
+    from abm_gb300.batched import BatchedSweep, sweep_instances
+    from abm_gb300.params import VFParams
+    lib = _lib.load()
+    kw = {} if fov is None else {"fov": fov}
+    vp = VFParams(alp1=0.08, bet1=0.08, width=width, height=width, rv=1200, **kw)
+    inst = sweep_instances(n_instances=9, n_min=10, n_max=260, alp_grid=(3, 3), seed=31,
+                           width=width, height=width)
+    cull = 10.0 / math.tan(2 * math.pi / 1200)   # h >= 1 only within this distance (R = 10)
+    assert (2 * width * width <= cull * cull) == (width < 1000.0)
+    outs = []
+    try:
+        for mode in (1, 3):
+            _lib.check(lib.abm_vpf_set_step_mode(mode, 1))
+            b = BatchedSweep(vp, inst)
+            for _ in range(2):
+                b.step(want_vpf=True, want_terms=True)
+            outs.append((b.vpf_numpy(), b.terms.cpu().numpy(), b.state_numpy()))
+    finally:
+        lib.abm_vpf_set_step_mode(0, 1)
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    for k in outs[0][2]:
+        assert np.array_equal(outs[0][2][k], outs[1][2][k]), k
