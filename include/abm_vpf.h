@@ -175,7 +175,7 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
  * agents are scheduled (put the largest instances first for load balance).  All instances share
  * p (Rv, arena, boundary, GAM, ALP1, BET1 ...).  Results per instance are bit-identical to
  * abm_vpf_flock_step on that instance alone.  Uses the group form of the pair kernel (groups
- * of 4 consecutive entries of the order) where it applies (walls, equal radii) and the L1 form
+ * of 8 consecutive entries of the order) where it applies (walls, equal radii) and the L1 form
  * otherwise, unless abm_vpf_set_step_mode selects one.
  */
 int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32_t n_total,
@@ -388,8 +388,8 @@ int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile);
  * group form where it applies, else the L1 form; the tiled form beyond), 1 = L1 form (one
  * block per focal agent, neighbours read through the read-only L1 path), 2 = tiled form
  * (warps_per_block focal agents share TMA-staged neighbour tiles), 3 = group form (one warp
- * per group of 4 consecutive focal agents, each neighbour read once for the group; one swarm
- * with walls and equal radii only, otherwise the step returns ABM_ERR_UNSUPPORTED).
+ * per group of 4 consecutive focal agents, 8 in a batched sweep, each neighbour read once for
+ * the group; walls and equal radii only, otherwise the step returns ABM_ERR_UNSUPPORTED).
  * warps_per_agent in {1, 2, 4} splits one focal agent's neighbours over that many warps in the
  * L1 form; 0 keeps the current value.  All forms give bit-identical results. */
 int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent);

@@ -55,7 +55,7 @@ def test_batched_step_matches_single_instances():
 
 
 def test_batched_group_and_l1_forms_agree():
-    """The group form (4 consecutive entries of the schedule per warp, straddling instances)
+    """The group form (8 consecutive entries of the schedule per warp, straddling instances)
     and the L1 form give identical results for a sweep, also with a schedule that interleaves
     the instances' agents."""
     import torch
@@ -70,7 +70,7 @@ def test_batched_group_and_l1_forms_agree():
         for mode, shuffle in ((1, False), (3, False), (3, True)):
             _lib.check(lib.abm_vpf_set_step_mode(mode, 1))
             b = BatchedSweep(vp, inst)
-            if shuffle:   # a schedule whose groups of 4 mix agents of several instances
+            if shuffle:   # a schedule whose groups of 8 mix agents of several instances
                 perm = np.random.default_rng(2).permutation(b.n).astype(np.int32)
                 b.order = torch.as_tensor(perm, device="cuda")
             b.step(want_vpf=True, want_terms=True)
