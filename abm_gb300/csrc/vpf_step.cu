@@ -956,28 +956,24 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
 
     int qn = 0, q2n = 0, wqn = 0;
     const unsigned lt = (1u << lane) - 1u;
-    const bool pl = a.pair_loads != 0;
-    // one scan of a neighbour range [j0, n) for the group's agents in `members`: two adjacent
-    // neighbours per lane, 64 per round, one 8-byte load per coordinate when the state is
-    // 8-byte aligned (the pairs start at an even index)
+    // one scan of a neighbour range [j0, n) for the group's agents in `members`: two
+    // neighbours per lane, 64 per round -- j0 + 64 r + lane and j0 + 64 r + 32 + lane in round
+    // r (two coalesced loads per coordinate), so that a range's last round skips its second
+    // half when that holds no neighbour (sweep step 237.7 -> 233.4 us against adjacent pairs)
     auto scan = [&](const int j0, const int n, const unsigned members) {
-        auto load2 = [&](int jj, float2 &xv, float2 &yv) {
-            if (pl && jj + 1 < n) {
-                xv = __ldg(reinterpret_cast<const float2 *>(a.x + jj));
-                yv = __ldg(reinterpret_cast<const float2 *>(a.y + jj));
-            } else {
-                xv = make_float2(jj < n ? __ldg(a.x + jj) : 0.f, jj + 1 < n ? __ldg(a.x + jj + 1) : 0.f);
-                yv = make_float2(jj < n ? __ldg(a.y + jj) : 0.f, jj + 1 < n ? __ldg(a.y + jj + 1) : 0.f);
-            }
+        auto load2 = [&](int jb, float2 &xv, float2 &yv) {
+            const int ja = jb + lane, jc = jb + 32 + lane;
+            xv = make_float2(ja < n ? __ldg(a.x + ja) : 0.f, jc < n ? __ldg(a.x + jc) : 0.f);
+            yv = make_float2(ja < n ? __ldg(a.y + ja) : 0.f, jc < n ? __ldg(a.y + jc) : 0.f);
         };
-        const int jb0 = j0 & ~1;
         float2 xn2, yn2;
-        load2(jb0 + 2 * lane, xn2, yn2);
-        for (int jb = jb0; jb < n; jb += 64) {
+        load2(j0, xn2, yn2);
+        for (int jb = j0; jb < n; jb += 64) {
             const float2 xv = xn2, yv = yn2;
-            const int jj = jb + 2 * lane;
-            load2(jb + 64 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
-            const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
+            const int ja = jb + lane, jc = jb + 32 + lane;
+            load2(jb + 64, xn2, yn2);   // prefetch the next round through L1
+            const bool v0 = ja < n, v1 = jc < n;
+            const bool second = jb + 32 < n;   // warp-uniform
             for (int g = 0; g < G; ++g) {   // warp-uniform
                 if (!((members >> g) & 1u)) continue;
                 const float fx = fd[g].x, fy = fd[g].y;
@@ -986,21 +982,23 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
                 const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
                 const bool live0 = v0 && d2.x > 0.f && d2.x <= cull_r2;
                 const bool live1 = v1 && d2.y > 0.f && d2.y <= cull_r2;
-                const int tag = jj | (g << kGroupTagShift);
+                const int gt = g << kGroupTagShift;
                 if constexpr (DIRECT) {   // phase B on the lanes' own candidates
-                    group_candidate<FULLFOV>(fd, QEntry<false>::make(dx.x, dy.x, d2.x, tag),
+                    group_candidate<FULLFOV>(fd, QEntry<false>::make(dx.x, dy.x, d2.x, ja | gt),
                                              live0, q2, q2n, wq, wqn, vball, a, counters);
-                    group_candidate<FULLFOV>(fd, QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1),
-                                             live1, q2, q2n, wq, wqn, vball, a, counters);
+                    if (second)
+                        group_candidate<FULLFOV>(fd,
+                                                 QEntry<false>::make(dx.y, dy.y, d2.y, jc | gt),
+                                                 live1, q2, q2n, wq, wqn, vball, a, counters);
                 } else {
                     const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
                     const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
                     const int c0 = __popc(lm0);
                     if (live0)
-                        q[qn + __popc(lm0 & lt)] = QEntry<false>::make(dx.x, dy.x, d2.x, tag);
+                        q[qn + __popc(lm0 & lt)] = QEntry<false>::make(dx.x, dy.x, d2.x, ja | gt);
                     if (live1)
                         q[qn + c0 + __popc(lm1 & lt)] =
-                            QEntry<false>::make(dx.y, dy.y, d2.y, tag + 1);
+                            QEntry<false>::make(dx.y, dy.y, d2.y, jc | gt);
                     qn += c0 + __popc(lm1);
                     __syncwarp();
                     while (qn >= 32) {   // warp-uniform; at most two batches
