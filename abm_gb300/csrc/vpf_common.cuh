@@ -78,6 +78,13 @@ __device__ __forceinline__ dfl df_add(dfl a, dfl b) {
 }
 __device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
 __device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+// a + b for a float b: df_add(a, {b, 0}) without the operations on the zero low part (the same
+// value; only the sign of a zero low part can differ)
+__device__ __forceinline__ dfl df_add_f(dfl a, float b) {
+    dfl s = two_sum(a.hi, b);
+    s.lo += a.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
 __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
     dfl p = two_prod(a.hi, b.hi);
     p.lo = fmaf(a.hi, b.lo, p.lo);
@@ -681,9 +688,10 @@ __device__ __forceinline__ void df_sincos_df(dfl theta, const float4 *tab, dfl &
     const dfl r2 = df_mul(r, r);
     const dfl sixth = {1.666666716e-01f, -4.967053879e-09f};
     const dfl s_in = df_sub(sixth, df_mul(r2, dfl{8.333333768e-03f, -4.346172033e-10f}));
-    const dfl sr = df_mul(r, df_sub(dfl{1.f, 0.f}, df_mul(r2, s_in)));
-    const dfl c_in = df_sub(dfl{0.5f, 0.f}, df_mul(r2, dfl{4.166666791e-02f, -1.241763470e-09f}));
-    const dfl cr = df_sub(dfl{1.f, 0.f}, df_mul(r2, c_in));
+    const dfl sr = df_mul(r, df_add_f(df_neg(df_mul(r2, s_in)), 1.f));
+    const dfl c_in =
+        df_add_f(df_neg(df_mul(r2, dfl{4.166666791e-02f, -1.241763470e-09f})), 0.5f);
+    const dfl cr = df_add_f(df_neg(df_mul(r2, c_in)), 1.f);
     const float4 t = tab[k];
     const dfl ck = {t.x, t.y}, sk = {t.z, t.w};
     c = df_sub(df_mul(ck, cr), df_mul(sk, sr));
@@ -743,13 +751,12 @@ __device__ __forceinline__ UpdateOut update_agent_df(const UpdateDf &p, const fl
     const dfl zero = {0.f, 0.f};
     UpdateOut o;
     dfl ab = zero, ae = zero, bb = zero, be = zero, dv = zero, dpsi = zero;
-    const dfl vel = {vf, 0.f};
     if (p.phi_ok) {
         ab = df_mul(alp0, df_neg(df_from_fix(bc)));
         ae = df_mul(df_mul(alp0, p.alp1), df_from_fix(ec));
         bb = df_mul(bet0, df_neg(df_from_fix(bs)));
         be = df_mul(df_mul(bet0, p.bet1), df_from_fix(es));
-        dv = df_add(df_add(df_mul(p.gam, df_sub(v0, vel)), ab), ae);
+        dv = df_add(df_add(df_mul(p.gam, df_add_f(v0, -vf)), ab), ae);
         dpsi = df_add(bb, be);
     }
     o.terms[0] = dv;
@@ -761,48 +768,46 @@ __device__ __forceinline__ UpdateOut update_agent_df(const UpdateDf &p, const fl
     dfl theta = df_mul(dpsi, p.dt);
     if (p.limit && df_lt(p.max_th, dfl{fabsf(theta.hi), theta.hi < 0 ? -theta.lo : theta.lo}))
         theta = (df_sign(theta) < 0) ? df_neg(p.max_th) : p.max_th;
-    dfl th = df_prove_orientation(df_add(dfl{thf, 0.f}, theta));
-    dfl v = df_add(vel, df_mul(dv, p.dt));
+    dfl th = df_prove_orientation(df_add_f(theta, thf));
+    dfl v = df_add_f(df_mul(dv, p.dt), vf);
     if (p.limit && df_lt(p.max_vel, dfl{fabsf(v.hi), v.hi < 0 ? -v.lo : v.lo}))
         v = (df_sign(v) < 0) ? df_neg(p.max_vel) : p.max_vel;
     dfl cs, sn;
     df_sincos_df(th, sctab, cs, sn);
     const dfl vdt = df_mul(v, p.dt);
-    dfl x = df_add(dfl{xf, 0.f}, df_mul(vdt, cs));
-    dfl y = df_sub(dfl{yf, 0.f}, df_mul(vdt, sn));
-    const dfl R = {Rf, 0.f};
-    const dfl cx = df_add(x, R), cy = df_add(y, R);
-    const dfl one = {1.f, 0.f};
+    dfl x = df_add_f(df_mul(vdt, cs), xf);
+    dfl y = df_add_f(df_neg(df_mul(vdt, sn)), yf);
+    const dfl cx = df_add_f(x, Rf), cy = df_add_f(y, Rf);
     if (!p.torus) {
         if (df_lt(cx, p.bx0)) {
-            x = df_sub(p.bx0, R);
+            x = df_add_f(p.bx0, -Rf);
             if (df_le(half_pi, th) && df_lt(th, pi)) th = df_sub(th, half_pi);
             else if (df_le(pi, th) && df_le(th, three_half_pi)) th = df_add(th, half_pi);
             th = df_prove_orientation(th);
         }
         if (df_lt(p.bx1, cx)) {
-            x = df_sub(df_sub(p.bx1, R), one);
+            x = df_add_f(df_add_f(p.bx1, -Rf), -1.f);
             if (df_le(three_half_pi, th) && df_lt(th, two_pi)) th = df_sub(th, half_pi);
             else if (df_le(zero, th) && df_le(th, half_pi)) th = df_add(th, half_pi);
             th = df_prove_orientation(th);
         }
         if (df_lt(cy, p.by0)) {
-            y = df_sub(p.by0, R);
+            y = df_add_f(p.by0, -Rf);
             if (df_le(half_pi, th) && df_le(th, pi)) th = df_add(th, half_pi);
             else if (df_le(zero, th) && df_lt(th, half_pi)) th = df_sub(th, half_pi);
             th = df_prove_orientation(th);
         }
         if (df_lt(p.by1, cy)) {
-            y = df_sub(df_sub(p.by1, R), one);
+            y = df_add_f(df_add_f(p.by1, -Rf), -1.f);
             if (df_le(three_half_pi, th) && df_le(th, two_pi)) th = df_add(th, half_pi);
             else if (df_le(pi, th) && df_lt(th, three_half_pi)) th = df_sub(th, half_pi);
             th = df_prove_orientation(th);
         }
     } else {
-        if (df_lt(cx, p.bx0)) x = df_sub(p.bx1, R);
-        else if (df_lt(p.bx1, cx)) x = df_add(p.bx0, R);
-        if (df_lt(cy, p.by0)) y = df_sub(p.by1, R);
-        else if (df_lt(p.by1, cy)) y = df_add(p.by0, R);
+        if (df_lt(cx, p.bx0)) x = df_add_f(p.bx1, -Rf);
+        else if (df_lt(p.bx1, cx)) x = df_add_f(p.bx0, Rf);
+        if (df_lt(cy, p.by0)) y = df_add_f(p.by1, -Rf);
+        else if (df_lt(p.by1, cy)) y = df_add_f(p.by0, Rf);
     }
     o.x = x.hi + x.lo;
     o.y = y.hi + y.lo;
