@@ -662,15 +662,16 @@ __device__ __forceinline__ void df_sincos(float theta, const float4 *tab, dfl &c
     const dfl H = {6.135923322e-03f, -1.707476105e-10f};      // 2 pi / 1024 in double-float
     const float kf = rintf(theta * inv_h);
     int k = (int)kf;
-    dfl r = df_sub(dfl{theta, 0.f}, df_add(two_prod(kf, H.hi), two_prod(kf, H.lo)));
+    dfl r = df_add_f(df_neg(df_add(two_prod(kf, H.hi), two_prod(kf, H.lo))), theta);
     k &= (kSinCosTab - 1);
     const dfl r2 = df_mul(r, r);
     // sin r = r (1 - r2 (1/6 - r2/120)),  cos r = 1 - r2 (1/2 - r2/24)
     const dfl sixth = {1.666666716e-01f, -4.967053879e-09f};
     const dfl s_in = df_sub(sixth, df_mul(r2, dfl{8.333333768e-03f, -4.346172033e-10f}));
-    const dfl sr = df_mul(r, df_sub(dfl{1.f, 0.f}, df_mul(r2, s_in)));
-    const dfl c_in = df_sub(dfl{0.5f, 0.f}, df_mul(r2, dfl{4.166666791e-02f, -1.241763470e-09f}));
-    const dfl cr = df_sub(dfl{1.f, 0.f}, df_mul(r2, c_in));
+    const dfl sr = df_mul(r, df_add_f(df_neg(df_mul(r2, s_in)), 1.f));
+    const dfl c_in =
+        df_add_f(df_neg(df_mul(r2, dfl{4.166666791e-02f, -1.241763470e-09f})), 0.5f);
+    const dfl cr = df_add_f(df_neg(df_mul(r2, c_in)), 1.f);
     const float4 t = tab[k];
     const dfl ck = {t.x, t.y}, sk = {t.z, t.w};
     c = df_sub(df_mul(ck, cr), df_mul(sk, sr));
