@@ -764,7 +764,9 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_kernel(const StepArgs 
     off += (size_t)kQueueW * sizeof(int2);
     unsigned *counters = reinterpret_cast<unsigned *>(smem + off);
 
-    for (int w = lane; w < G * words; w += 32) vball[w] = 0u;
+    // the bitmasks, 16 bytes per store (their region is padded to 16 bytes)
+    for (int w4 = lane; 4 * w4 < G * words; w4 += 32)
+        reinterpret_cast<uint4 *>(vball)[w4] = make_uint4(0u, 0u, 0u, 0u);
     if (lane < 4) counters[lane] = 0u;
     allow_dependent_launch();
     if (lane < G) fd[lane] = load_focal<false>(a, i0 + lane);   // the group's agents at once
@@ -941,7 +943,9 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
     off += (size_t)kQueueW * sizeof(int2);
     unsigned *counters = reinterpret_cast<unsigned *>(smem + off);
 
-    for (int w = lane; w < G * words; w += 32) vball[w] = 0u;
+    // the bitmasks, 16 bytes per store (their region is padded to 16 bytes)
+    for (int w4 = lane; 4 * w4 < G * words; w4 += 32)
+        reinterpret_cast<uint4 *>(vball)[w4] = make_uint4(0u, 0u, 0u, 0u);
     if (lane < 4) counters[lane] = 0u;
     allow_dependent_launch();
     if (lane < G) {   // the group's agents at once
