@@ -52,7 +52,7 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM traffic of one launch of the dominant kernel (the group-form pair kernel) of this
 # workload, from the ncu capture summarised in profiles/vpf_pairs_group_n4096_rv3600.md
 # (dram__bytes_read.sum + dram__bytes_write.sum).
-NCU_TRAFFIC_BYTES = 2009100
+NCU_TRAFFIC_BYTES = 2009088
 
 
 def make_workload(seed=WORKLOAD["seed"], n=WORKLOAD["n_agents"]):
