@@ -252,38 +252,53 @@ static NoAllocDevice *noalloc_device(int *status) {
     return &devs[dev];
 }
 
-// Double-float re-decision of one deferred pair (xj, yj, rj: the neighbour's position and
-// radius) and its rasterisation; returns whether a re-decided boundary lies within 1e-9 rad
-// of the pair's edge angle.
-template <bool TORUS, bool HETERO>
-__device__ __forceinline__ bool resolve_and_raster(const FocalDev &f, float xj, float yj, float rj,
-                                                   uint32_t *vb, const StepArgs &a) {
-    float dx, dy;
-    pair_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, dx, dy);
-    const PairEst de = estimate_pair<HETERO>(f, dx, dy, rj, HETERO ? rcp_approx(rj) : f.invr,
-                                             a.g);
-    dfl ex, ey;
-    exact_offset<TORUS, HETERO>(f, xj, yj, rj, a.W, a.H, ex, ey);
-    const int3 th = resolve_pair(f.cd, f.sd, ex, ey, rj, resolve_grid(a.g), de.unc_t, de.unc_h,
-                                 de.u, de.ps2, de.t, de.h);
-    const int ds = th.x - th.y, dn = th.x + th.y;
-    if (projection_visible(a.g, ds, dn)) raster_fast(vb, a.g.rv, ds, dn);
-    return th.z != 0;
+// The rare paths of the per-agent forms (L1 and tiled), out of line so that the inlined copies
+// of phase B stay small, as in the group forms.
+//
+// 32 queued long or wrapping runs of one agent's bitmask (one per lane) through the general
+// fill.
+static __device__ __noinline__ void drain_runs_one(const int2 *wq, uint32_t *vb, int rv) {
+    const int lane = threadIdx.x & 31;
+    const int2 r = wq[lane];
+    raster_projection(vb, rv, r.x, r.y);
 }
 
-// The neighbour a deferred queue entry stands for: position and radius.
-template <bool HETERO>
-__device__ __forceinline__ void deferred_neighbour(const QEntry<HETERO> &d, const StepArgs &a,
-                                                   float &xj, float &yj, float &rj) {
-    if constexpr (HETERO) {
-        xj = d.x();
-        yj = d.y();
-        rj = d.r(a.radius0);
-    } else {
-        xj = __ldg(a.x + d.j());
-        yj = __ldg(a.y + d.j());
-        rj = a.radius0;
+// Double-float re-decision and rasterisation of focal agent f's deferred pairs qe[0 .. cnt)
+// (one per lane); returns the ballot of the pairs with a re-decided boundary within 1e-9 rad of
+// their edge angle.
+template <bool TORUS, bool HETERO>
+static __device__ __noinline__ unsigned drain_deferred_one(const FocalDev f,
+                                                           const QEntry<HETERO> *qe, int cnt,
+                                                           uint32_t *vb, const float *x,
+                                                           const float *y, float R0, dfl W,
+                                                           dfl H, GridDev g) {
+    const int lane = threadIdx.x & 31;
+    bool near = false;
+    if (lane < cnt) {
+        float xj, yj, rj;
+        if constexpr (HETERO) {
+            xj = qe[lane].x();
+            yj = qe[lane].y();
+            rj = qe[lane].r(R0);
+        } else {
+            const int j = qe[lane].j();
+            xj = __ldg(x + j);
+            yj = __ldg(y + j);
+            rj = R0;
+        }
+        float dx, dy;
+        pair_offset<TORUS, HETERO>(f, xj, yj, rj, W, H, dx, dy);
+        const PairEst de = estimate_pair<HETERO>(f, dx, dy, rj, HETERO ? rcp_approx(rj) : f.invr,
+                                                 g);
+        dfl ex, ey;
+        exact_offset<TORUS, HETERO>(f, xj, yj, rj, W, H, ex, ey);
+        const int3 th = resolve_pair(f.cd, f.sd, ex, ey, rj, resolve_grid(g), de.unc_t,
+                                     de.unc_h, de.u, de.ps2, de.t, de.h);
+        const int ds = th.x - th.y, dn = th.x + th.y;
+        if (projection_visible(g, ds, dn)) raster_fast(vb, g.rv, ds, dn);
+        near = th.z != 0;
     }
+    return __ballot_sync(ABM_FULL_MASK, near);
 }
 
 // Heavy decision + rasterisation of up to 32 queued candidates (lane < cnt holds one).
@@ -318,8 +333,7 @@ __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEnt
             __syncwarp();
             if (wqn >= 32) {
                 wqn -= 32;
-                const int2 r = wq[wqn + lane];
-                raster_projection(vb, a.g.rv, r.x, r.y);
+                drain_runs_one(wq + wqn, vb, a.g.rv);
                 __syncwarp();
             }
         }
@@ -342,10 +356,8 @@ __device__ __forceinline__ void process_candidates(const FocalDev &f, const QEnt
     __syncwarp();
     if (q2n >= 32) {   // drain 32 deferred pairs (warp-uniform)
         q2n -= 32;
-        float xj, yj, rj;
-        deferred_neighbour<HETERO>(q2[q2n + lane], a, xj, yj, rj);
-        const bool near = resolve_and_raster<TORUS, HETERO>(f, xj, yj, rj, vb, a);
-        const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
+        const unsigned nm = drain_deferred_one<TORUS, HETERO>(f, q2 + q2n, 32, vb, a.x, a.y,
+                                                              a.radius0, a.W, a.H, a.g);
         if (lane == 0) {
             atomicAdd(cnt_resolved, 32u);
             if (nm) atomicAdd(cnt_near, (unsigned)__popc(nm));
@@ -372,13 +384,8 @@ __device__ __forceinline__ void drain_deferred(const FocalDev &f, const QEntry<H
                                                unsigned *cnt_resolved, unsigned *cnt_near) {
     const int lane = threadIdx.x & 31;
     if (q2n == 0) return;
-    bool near = false;
-    if (lane < q2n) {
-        float xj, yj, rj;
-        deferred_neighbour<HETERO>(q2[lane], a, xj, yj, rj);
-        near = resolve_and_raster<TORUS, HETERO>(f, xj, yj, rj, vb, a);
-    }
-    const unsigned nm = __ballot_sync(ABM_FULL_MASK, near);
+    const unsigned nm = drain_deferred_one<TORUS, HETERO>(f, q2, q2n, vb, a.x, a.y, a.radius0,
+                                                          a.W, a.H, a.g);
     if (lane == 0) {
         atomicAdd(cnt_resolved, (unsigned)q2n);
         if (nm) atomicAdd(cnt_near, (unsigned)__popc(nm));
