@@ -1,15 +1,18 @@
 // vpf_step.cu -- the per-timestep hot path (VPF rasterisation + VSWRM integrals + agent update)
 // and the drop-in twins of projection_field / VSWRM_flocking_state_variables.
 //
-// One step is two launches.  The pair kernel runs one warp per focal agent: it evaluates every
-// neighbour (FP32 with a guard band and a double-float re-decision inside it), OR-s the visible
-// pixel runs into the agent's VPF bitmask in shared memory and reduces the bitmask's
-// transitions to the four VSWRM sums (fixed point).  The update kernel then applies the
-// reference's heading / speed / position update and boundary rule, one thread per agent, in
-// double-float arithmetic on the FP32 pipe (GB300's FP64 rate is a small fraction of its FP32
-// rate).  Two forms of the pair kernel:
-//  * `l1`: single-warp blocks, neighbours read through the read-only L1 path; about 27 agents
-//    per SM and no block barriers;
+// One step is two launches.  The pair kernel evaluates every neighbour of its focal agents
+// (FP32 with a guard band and a double-float re-decision inside it), OR-s the visible pixel runs
+// into each agent's VPF bitmask in shared memory and reduces the bitmask's transitions to the
+// four VSWRM sums (fixed point).  The second kernel (the update kernel, or the finish kernel
+// after a pair kernel split into neighbour chunks, which also reduces the sums) applies the
+// reference's heading / speed / position update and boundary rule in double-float arithmetic
+// on the FP32 pipe (GB300's FP64 rate is a small fraction of its FP32 rate).  Forms of the
+// pair kernel:
+//  * `group`: one warp per group of 4 consecutive agents of one swarm (8 entries of a batched
+//    sweep's schedule), each neighbour read once for the group (walls, equal radii);
+//  * `l1`: single-warp blocks, one focal agent each, neighbours read through the read-only L1
+//    path (per-agent radii, the torus);
 //  * `tiled`: several focal warps per block share neighbour tiles staged in shared memory by the
 //    TMA bulk engine (double-buffered with mbarriers), for swarms whose positions exceed L1.
 #include <algorithm>
