@@ -10,9 +10,10 @@
 // on the FP32 pipe (GB300's FP64 rate is a small fraction of its FP32 rate).  Forms of the
 // pair kernel:
 //  * `group`: one warp per group of 4 consecutive agents of one swarm (8 entries of a batched
-//    sweep's schedule), each neighbour read once for the group (walls, equal radii);
+//    sweep's schedule), each neighbour read once for the group (equal radii; walls, and for one
+//    swarm the torus whose width and height are floats);
 //  * `l1`: single-warp blocks, one focal agent each, neighbours read through the read-only L1
-//    path (per-agent radii, the torus);
+//    path (per-agent radii, the other tori);
 //  * `tiled`: several focal warps per block share neighbour tiles staged in shared memory by the
 //    TMA bulk engine (double-buffered with mbarriers), for swarms whose positions exceed L1.
 #include <algorithm>
@@ -596,7 +597,8 @@ __global__ void __launch_bounds__(32 * WPA) vpf_pairs_l1_kernel(const StepArgs a
 }
 
 // ---------------------------------------------------------------------------- group form
-// One warp serves kGroup consecutive focal agents of a single swarm (walls, equal radii):
+// One warp serves kGroup consecutive focal agents of a single swarm (equal radii; walls, or a
+// torus whose width and height are floats):
 // phase A reads each neighbour once for the whole group, and the candidate queue mixes the
 // group's agents -- each entry carries the agent's slot in the group in the top byte of its
 // neighbour index -- so the batches of phase B stay full, and the per-block costs (focal
@@ -636,11 +638,14 @@ static __device__ __noinline__ void drain_run_queue(const int2 *wq, uint32_t *vb
 }
 
 // Double-float re-decision and rasterisation of the deferred pairs qe[0 .. cnt) (one per lane;
-// equal radii R, walls); returns the ballot of the pairs with a re-decided boundary within
-// 1e-9 rad of their edge angle.
-static __device__ __noinline__ unsigned drain_deferred(const FocalDev *fd, const QEntry<false> *qe,
-                                                       int cnt, uint32_t *vball, const float *x,
-                                                       const float *y, float R, GridDev g) {
+// equal radii R; TORUS: the minimal image on the W x H torus); returns the ballot of the pairs
+// with a re-decided boundary within 1e-9 rad of their edge angle.
+template <bool TORUS>
+__device__ __forceinline__ unsigned drain_deferred_body(const FocalDev *fd,
+                                                        const QEntry<false> *qe, int cnt,
+                                                        uint32_t *vball, const float *x,
+                                                        const float *y, float R, dfl W, dfl H,
+                                                        GridDev g) {
     const int lane = threadIdx.x & 31;
     bool near = false;
     if (lane < cnt) {
@@ -649,12 +654,11 @@ static __device__ __noinline__ unsigned drain_deferred(const FocalDev *fd, const
         const int j = tag & ((1 << kGroupTagShift) - 1);
         const FocalDev &f = fd[dg];
         const float xj = __ldg(x + j), yj = __ldg(y + j);
-        const dfl z = {0.f, 0.f};
         float dx, dy;
-        pair_offset<false, false>(f, xj, yj, R, z, z, dx, dy);
+        pair_offset<TORUS, false>(f, xj, yj, R, W, H, dx, dy);
         const PairEst de = estimate_pair<false>(f, dx, dy, R, f.invr, g);
         dfl ex, ey;
-        exact_offset<false, false>(f, xj, yj, R, z, z, ex, ey);
+        exact_offset<TORUS, false>(f, xj, yj, R, W, H, ex, ey);
         const int3 th = resolve_pair(f.cd, f.sd, ex, ey, R, resolve_grid(g), de.unc_t, de.unc_h,
                                      de.u, de.ps2, de.t, de.h);
         const int ds = th.x - th.y, dn = th.x + th.y;
@@ -664,11 +668,61 @@ static __device__ __noinline__ unsigned drain_deferred(const FocalDev *fd, const
     return __ballot_sync(ABM_FULL_MASK, near);
 }
 
+static __device__ __noinline__ unsigned drain_deferred(const FocalDev *fd, const QEntry<false> *qe,
+                                                       int cnt, uint32_t *vball, const float *x,
+                                                       const float *y, float R, GridDev g) {
+    const dfl z = {0.f, 0.f};
+    return drain_deferred_body<false>(fd, qe, cnt, vball, x, y, R, z, z, g);
+}
+
+static __device__ __noinline__ unsigned drain_deferred_torus(const FocalDev *fd,
+                                                             const QEntry<false> *qe, int cnt,
+                                                             uint32_t *vball, const float *x,
+                                                             const float *y, float R, dfl W,
+                                                             dfl H, GridDev g) {
+    return drain_deferred_body<true>(fd, qe, cnt, vball, x, y, R, W, H, g);
+}
+
+// The minimal torus image (vf_supcalc.py:70-83) of two FP32 offsets d = fl(v - f) along one
+// axis of length L, a float (its double-float low part is zero); the result is the wrapped
+// exact offset rounded once, as the double-float offset gives it.  The exact offset is d + e
+// (e: the two-sum error).  It wraps iff it lies beyond +-L/2: L/2 is a float, d - L/2 is exact
+// wherever the sign of the sum is in doubt (Sterbenz), so fl(fl(d -+ L/2) + e) has the sign of
+// the exact comparison.  A wrapped offset is fl(fl(d -+ L) + e), exact up to the last rounding
+// for |d| <= 2L; `far` flags the offsets beyond that (positions more than 2L apart), which the
+// caller takes through the double-float offset.  An offset that does not wrap stays d, since
+// fl(d + e) = d.
+__device__ __forceinline__ float2 torus_image2(float2 d, float2 v, float f, float L, bool &far) {
+    const float2 nb = __fadd2_rn(v, make_float2(-d.x, -d.y));   // v - d
+    const float2 t = __fadd2_rn(d, nb);                          // d - (d - v)
+    const float2 e = __fadd2_rn(__fadd2_rn(v, make_float2(-t.x, -t.y)),
+                                __fadd2_rn(make_float2(-f, -f), nb));
+    const float h = 0.5f * L;
+    const float2 up = __fadd2_rn(__fadd2_rn(d, make_float2(-h, -h)), e);
+    const float2 dn = __fadd2_rn(__fadd2_rn(d, make_float2(h, h)), e);
+    const float wx = up.x > 0.f ? L : (dn.x < 0.f ? -L : 0.f);
+    const float wy = up.y > 0.f ? L : (dn.y < 0.f ? -L : 0.f);
+    far = fabsf(d.x) > 2.f * L || fabsf(d.y) > 2.f * L;
+    return __fadd2_rn(__fadd2_rn(d, make_float2(-wx, -wy)), e);
+}
+
+// The offsets of the two neighbours (xv, yv) from focal agent f through the double-float
+// minimal image (the rare far offsets of torus_image2), as the one-block form computes them.
+static __device__ __noinline__ float4 torus_offsets_exact(const FocalDev *fd, int g, float2 xv,
+                                                          float2 yv, dfl W, dfl H) {
+    const FocalDev &f = fd[g];
+    float4 r;
+    pair_offset<true, false>(f, xv.x, yv.x, f.r, W, H, r.x, r.z);
+    pair_offset<true, false>(f, xv.y, yv.y, f.r, W, H, r.y, r.w);
+    return r;
+}
+
 // Phase B of one (agent slot, neighbour) candidate per lane (`have`: the lane holds one; e: its
 // offset, d^2 and tagged neighbour index): FP32 decisions, rasterisation of short runs, long and
 // wrapping runs to the run queue, guard-band pairs to the double-float queue (each drained 32
 // at a time).  FULLFOV: the field of view is the whole circle, so every projection is visible.
-template <bool FULLFOV>
+// TORUS: the offsets are minimal torus images (the deferred pairs recompute theirs).
+template <bool FULLFOV, bool TORUS = false>
 __device__ __forceinline__ void group_candidate(const FocalDev *fd, const QEntry<false> &e,
                                                 bool have, QEntry<false> *q2, int &q2n, int2 *wq,
                                                 int &wqn, uint32_t *vball, const StepArgs &a,
@@ -716,8 +770,12 @@ __device__ __forceinline__ void group_candidate(const FocalDev *fd, const QEntry
         __syncwarp();
         if (q2n >= 32) {   // drain 32 deferred pairs (warp-uniform)
             q2n -= 32;
-            const unsigned nm =
-                drain_deferred(fd, q2 + q2n, 32, vball, a.x, a.y, a.radius0, a.g);
+            unsigned nm;
+            if constexpr (TORUS)
+                nm = drain_deferred_torus(fd, q2 + q2n, 32, vball, a.x, a.y, a.radius0, a.W, a.H,
+                                          a.g);
+            else
+                nm = drain_deferred(fd, q2 + q2n, 32, vball, a.x, a.y, a.radius0, a.g);
             if (lane == 0) {
                 atomicAdd(&counters[0], 32u);
                 if (nm) atomicAdd(&counters[1], (unsigned)__popc(nm));
@@ -728,7 +786,7 @@ __device__ __forceinline__ void group_candidate(const FocalDev *fd, const QEntry
 }
 
 // Phase B of up to 32 queued candidates (lane < cnt holds one).
-template <bool FULL, bool FULLFOV>
+template <bool FULL, bool FULLFOV, bool TORUS = false>
 __device__ __forceinline__ void group_batch(const FocalDev *fd, const QEntry<false> *q, int cnt,
                                             QEntry<false> *q2, int &q2n, int2 *wq, int &wqn,
                                             uint32_t *vball, const StepArgs &a,
@@ -736,12 +794,13 @@ __device__ __forceinline__ void group_batch(const FocalDev *fd, const QEntry<fal
     const int lane = threadIdx.x & 31;
     const bool have = FULL || lane < cnt;
     const QEntry<false> e = (FULL || have) ? q[lane] : QEntry<false>::make(1.f, 0.f, 1.f, 0);
-    group_candidate<FULLFOV>(fd, e, have, q2, q2n, wq, wqn, vball, a, counters);
+    group_candidate<FULLFOV, TORUS>(fd, e, have, q2, q2n, wq, wqn, vball, a, counters);
 }
 
 // The group form for one swarm: the group is 4 consecutive agents, the neighbours the block's
-// chunk.
-template <bool FULLFOV>
+// chunk.  TORUS: the minimal images on a torus whose width and height are floats (N=4096 torus
+// step 166.6 -> 102.8 us against the l1 form, bit-identical).
+template <bool FULLFOV, bool TORUS = false>
 __global__ void __launch_bounds__(32, 32) vpf_pairs_group_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x;
@@ -807,8 +866,19 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_kernel(const StepArgs 
         const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
         for (int g = 0; g < G; ++g) {   // warp-uniform
             const float fx = fd[g].x, fy = fd[g].y;
-            const float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
-            const float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
+            float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
+            float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
+            if constexpr (TORUS) {
+                bool farx, fary;
+                dx = torus_image2(dx, xv, fx, a.W.hi, farx);
+                dy = torus_image2(dy, yv, fy, a.H.hi, fary);
+                const bool far = (v0 || v1) && (farx || fary);
+                if (__any_sync(ABM_FULL_MASK, far) && far) {
+                    const float4 o = torus_offsets_exact(fd, g, xv, yv, a.W, a.H);
+                    dx = make_float2(o.x, o.y);
+                    dy = make_float2(o.z, o.w);
+                }
+            }
             const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
             const bool live0 = v0 && d2.x > 0.f && d2.x <= cull_r2;
             const bool live1 = v1 && d2.y > 0.f && d2.y <= cull_r2;
@@ -823,11 +893,13 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_kernel(const StepArgs 
             __syncwarp();
             while (qn >= 32) {   // warp-uniform; at most two batches
                 qn -= 32;
-                group_batch<true, FULLFOV>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a, counters);
+                group_batch<true, FULLFOV, TORUS>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a,
+                                                  counters);
             }
         }
     }
-    if (qn > 0) group_batch<false, FULLFOV>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
+    if (qn > 0)
+        group_batch<false, FULLFOV, TORUS>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
     if (lane < wqn) {   // the last long or wrapping runs
         const int2 r = wq[lane];
         raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
@@ -835,8 +907,13 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_kernel(const StepArgs 
     }
     __syncwarp();
     // the last (< 32) deferred pairs
-    const unsigned nm =
-        q2n ? drain_deferred(fd, q2, q2n, vball, a.x, a.y, a.radius0, a.g) : 0u;
+    unsigned nm = 0u;
+    if (q2n) {
+        if constexpr (TORUS)
+            nm = drain_deferred_torus(fd, q2, q2n, vball, a.x, a.y, a.radius0, a.W, a.H, a.g);
+        else
+            nm = drain_deferred(fd, q2, q2n, vball, a.x, a.y, a.radius0, a.g);
+    }
     if (lane == 0 && q2n) {
         counters[0] += (unsigned)q2n;
         counters[1] += (unsigned)__popc(nm);
@@ -1534,7 +1611,8 @@ static int chunk_plan(int n, int c, int *off) {
     return r;
 }
 
-// group form (walls, equal radii, one swarm): chunks as in launch_l1, counted in groups.
+// group form (equal radii; one swarm, or walls in a batched sweep): chunks as in launch_l1,
+// counted in groups.
 static int launch_group(StepArgs a, int split, double arena_w, double arena_h,
                         cudaStream_t stream, int *chunks) {
     const int gsz = a.seg_begin ? kSegGroup : kGroup;
@@ -1581,8 +1659,11 @@ static int launch_group(StepArgs a, int split, double arena_w, double arena_h,
         else if (direct) e = launch_pdl(vpf_pairs_group_seg_kernel<false, true>, blocks, 32, smem, stream, a);
         else e = launch_pdl(vpf_pairs_group_seg_kernel<false, false>, blocks, 32, smem, stream, a);
     } else {
-        e = ff ? launch_pdl(vpf_pairs_group_kernel<true>, blocks, 32, smem, stream, a)
-               : launch_pdl(vpf_pairs_group_kernel<false>, blocks, 32, smem, stream, a);
+        const bool torus = a.ud.torus != 0;
+        if (ff && !torus) e = launch_pdl(vpf_pairs_group_kernel<true, false>, blocks, 32, smem, stream, a);
+        else if (!torus) e = launch_pdl(vpf_pairs_group_kernel<false, false>, blocks, 32, smem, stream, a);
+        else if (ff) e = launch_pdl(vpf_pairs_group_kernel<true, true>, blocks, 32, smem, stream, a);
+        else e = launch_pdl(vpf_pairs_group_kernel<false, true>, blocks, 32, smem, stream, a);
     }
     return check_cuda(e, "vpf_pairs_group_kernel launch");
 }
@@ -1929,10 +2010,13 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     const bool hetero = a.radius != nullptr;
     // auto: the l1 form while the positions fit comfortably in L1, tiled beyond; segmented
     // (batched) swarms always use the l1 form
-    const bool group_ok = !torus && !hetero && n < (1 << kGroupTagShift);
+    // the group form: equal radii; on a torus one swarm whose width and height are floats
+    const bool group_ok = !hetero && n < (1 << kGroupTagShift) &&
+                          (!torus || (!seg_begin && a.W.lo == 0.f && a.H.lo == 0.f));
     if (mode == 3 && !group_ok)
-        return set_error(ABM_ERR_UNSUPPORTED, "%s: the group form needs walls and equal radii",
-                         fn);
+        return set_error(ABM_ERR_UNSUPPORTED,
+                         "%s: the group form needs equal radii (on a torus: one swarm, width and "
+                         "height exact in float32)", fn);
     // automatic: the group form for one swarm up to 16384 agents and for batched sweeps
     const bool use_group = group_ok && (mode == 3 || (mode == 0 && (seg_begin || n <= 16384)));
     const bool use_l1 = !use_group && (seg_begin || mode == 1 || (mode == 0 && n <= 16384));

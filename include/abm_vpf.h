@@ -281,8 +281,9 @@ int abm_vpf_flock_run_recorded(abm_swarm_state *a, abm_swarm_state *b, int32_t n
  * double-float sincos table) lives in a file-scope device array of about 2.5 MiB that every GPU
  * loading the library holds until the process exits; no cudaMalloc, cudaFree or other
  * allocating routine is called.  Up to 16384 agents it runs the group pair kernel without
- * neighbour chunks (walls, equal radii) or the one-block-per-agent one, above that the tiled
- * one (none of them needs the bitmask workspace of the split form).
+ * neighbour chunks (equal radii; walls, or a torus whose width and height are exact in
+ * float32) or the one-block-per-agent one, above that the tiled one (none of them needs the
+ * bitmask workspace of the split form).
  * Limits: n <= ABM_NOALLOC_MAX_AGENTS and rv <= ABM_NOALLOC_MAX_RV, larger values return
  * ABM_ERR_INVALID_ARG / ABM_ERR_RV with a message.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) and copies the sincos table into it, and a call
@@ -389,7 +390,8 @@ int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile);
  * block per focal agent, neighbours read through the read-only L1 path), 2 = tiled form
  * (warps_per_block focal agents share TMA-staged neighbour tiles), 3 = group form (one warp
  * per group of 4 consecutive focal agents, 8 in a batched sweep, each neighbour read once for
- * the group; walls and equal radii only, otherwise the step returns ABM_ERR_UNSUPPORTED).
+ * the group; equal radii, and on the infinite (torus) arena only for one swarm whose width
+ * and height are exact in float32; otherwise the step returns ABM_ERR_UNSUPPORTED).
  * warps_per_agent in {1, 2, 4} splits one focal agent's neighbours over that many warps in the
  * L1 form; 0 keeps the current value.  All forms give bit-identical results. */
 int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent);

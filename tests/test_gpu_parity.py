@@ -249,6 +249,51 @@ def test_launch_configs_agree_torus_radii():
                             (2, 1, 8, 1024, 0)), radius=radius)
 
 
+@pytest.mark.parametrize("fov", [None, (-1.5, 2.0)])
+def test_group_form_torus_agrees(fov):
+    """The group form on the torus (equal radii) against the L1 and tiled forms, bit for bit:
+    a random swarm on a 1000 x 800 torus plus agents placed on the wrap seam (offsets of
+    exactly W/2 and H/2, and offsets W/2 +- 1e-5 whose float32 difference rounds to W/2, on
+    either side), two agents whose images coincide, and agents more than 2W or 2H from others
+    (the double-float offset's path)."""
+    from abm_gb300.params import VFParams
+    st = seeded_swarm(31, 1200, 1000.0, 800.0, pad=10.0, R=5.0)
+    seam = [(-1e-5, 200.0), (500.0, 210.0), (1e-5, 220.0), (100.0, 230.0), (600.0, 240.0),
+            (20.0, -1e-5), (30.0, 400.0), (40.0, 1e-5), (50.0, 50.0), (60.0, 450.0),
+            (0.0, 0.0), (1000.0, 0.0), (2600.0, 300.0), (300.0, 2000.0), (-2300.0, 500.0)]
+    rng = np.random.default_rng(31)
+    for k in ("x", "y"):
+        extra = np.array([p[0 if k == "x" else 1] for p in seam], dtype=np.float32)
+        st[k] = np.concatenate([st[k], extra])
+    m = len(seam)
+    st["theta"] = np.concatenate([st["theta"],
+                                  rng.uniform(0, 2 * np.pi, m).astype(np.float32)])
+    st["v"] = np.concatenate([st["v"], rng.uniform(0, 1.5, m).astype(np.float32)])
+    kw = {} if fov is None else {"fov": fov}
+    vp = VFParams(width=1000.0, height=800.0, rv=1200, radius=5.0, boundary="infinite", **kw)
+    _configs_agree(vp, st, ((1, 1, 8, 8192, 1), (3, 1, 8, 8192, 1), (3, 1, 8, 8192, 4),
+                            (0, 1, 8, 8192, 0), (1, 1, 8, 8192, 4), (2, 1, 8, 1024, 0)))
+
+
+def test_group_form_torus_needs_float_extent():
+    """A torus whose width is not exact in float32 is refused by the group form (the
+    automatic configuration then takes the L1 form)."""
+    from abm_gb300 import _lib
+    from abm_gb300.params import VFParams
+    from abm_gb300.swarm import VFSwarm
+    lib = _lib.load()
+    st = seeded_swarm(32, 200, 1000.0, 1000.0, pad=10.0, R=5.0)
+    vp = VFParams(width=1000.1, height=1000.0, rv=1200, radius=5.0, boundary="infinite")
+    try:
+        _lib.check(lib.abm_vpf_set_step_mode(3, 1))
+        s = VFSwarm(vp, st["x"], st["y"], st["theta"], st["v"])
+        with pytest.raises(Exception, match="group form"):
+            s.step()
+    finally:
+        lib.abm_vpf_set_step_mode(0, 1)
+    _configs_agree(vp, st, ((0, 1, 8, 8192, 0), (1, 1, 8, 8192, 1)))
+
+
 def test_split_workspace_is_clean_between_calls():
     """The split form's per-agent bitmasks in the stream workspace are zero again after every
     step: swarms of different sizes and Rv stepped one after another on one stream give the

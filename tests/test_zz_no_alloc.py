@@ -6,9 +6,10 @@ from a fixed file-scope scratch array.  This test calls both entry points throug
 calls in a row, with different swarm sizes and grids so each call has to replace the array's
 previous contents, and checks that the results agree within the parity tolerances the other GPU
 tests use (they are in fact expected to be bit-identical).  The cases cover the three pair
-kernels the entry point uses: up to 16384 agents the group form without neighbour chunks (walls,
-equal radii) and the one-block-per-agent form (the torus), above that the tiled form.  It also
-checks the size limits.  The file name makes pytest collect it last.
+kernels the entry point uses: up to 16384 agents the group form without neighbour chunks (walls;
+a torus whose width and height are exact in float32) and the one-block-per-agent form (a torus
+of another width), above that the tiled form.  It also checks the size limits.  The file name
+makes pytest collect it last.
 """
 import ctypes
 
@@ -58,6 +59,7 @@ def test_no_alloc_matches_regular_entry_point():
     lib = _lib.load()
     rng = np.random.default_rng(77)
     cases = [(3000, 3600, 5.0, 5000.0, "walls"), (700, 1200, 10.0, 600.0, "infinite"),
+             (500, 1200, 10.0, 600.3, "infinite"),   # not a float: the one-block form
              (20000, 1200, 3.0, 9000.0, "walls")]   # the last one: the tiled pair kernel
     for n, rv, R, W, boundary in cases:   # calls in a row, different grids and sizes
         state = {"x": rng.uniform(25, W + 25, n), "y": rng.uniform(25, W + 25, n),
