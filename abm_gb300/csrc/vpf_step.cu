@@ -10,8 +10,8 @@
 // on the FP32 pipe (GB300's FP64 rate is a small fraction of its FP32 rate).  Forms of the
 // pair kernel:
 //  * `group`: one warp per group of 4 consecutive agents of one swarm (8 entries of a batched
-//    sweep's schedule), each neighbour read once for the group (equal radii; walls, and for one
-//    swarm the torus whose width and height are floats);
+//    sweep's schedule), each neighbour read once for the group (equal radii; walls, or a torus
+//    whose width and height are floats);
 //  * `l1`: single-warp blocks, one focal agent each, neighbours read through the read-only L1
 //    path (per-agent radii, the other tori);
 //  * `tiled`: several focal warps per block share neighbour tiles staged in shared memory by the
@@ -1008,8 +1008,9 @@ __device__ __forceinline__ void group_finish_loop(const StepArgs &a, const int *
 // is scanned once for the agents that share it.  (A separate kernel: folding this into the
 // single-swarm kernel measured 1.3 us slower per step at N=4096.)  DIRECT: the arena lies
 // within the cull radius, so (almost) every pair is live and phase B takes the candidates
-// straight from the scan, without the queue that compacts the live ones.
-template <bool FULLFOV, bool DIRECT>
+// straight from the scan, without the queue that compacts the live ones.  TORUS: the minimal
+// images on a torus whose width and height are floats, as in the single-swarm kernel.
+template <bool FULLFOV, bool DIRECT, bool TORUS = false>
 __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int s_agent[kSegGroup], s_j0[kSegGroup], s_j1[kSegGroup];
@@ -1068,19 +1069,31 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
             for (int g = 0; g < G; ++g) {   // warp-uniform
                 if (!((members >> g) & 1u)) continue;
                 const float fx = fd[g].x, fy = fd[g].y;
-                const float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
-                const float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
+                float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
+                float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
+                if constexpr (TORUS) {
+                    bool farx, fary;
+                    dx = torus_image2(dx, xv, fx, a.W.hi, farx);
+                    dy = torus_image2(dy, yv, fy, a.H.hi, fary);
+                    const bool far = (v0 || v1) && (farx || fary);
+                    if (__any_sync(ABM_FULL_MASK, far) && far) {
+                        const float4 o = torus_offsets_exact(fd, g, xv, yv, a.W, a.H);
+                        dx = make_float2(o.x, o.y);
+                        dy = make_float2(o.z, o.w);
+                    }
+                }
                 const float2 d2 = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
                 const bool live0 = v0 && d2.x > 0.f && d2.x <= cull_r2;
                 const bool live1 = v1 && d2.y > 0.f && d2.y <= cull_r2;
                 const int gt = g << kGroupTagShift;
                 if constexpr (DIRECT) {   // phase B on the lanes' own candidates
-                    group_candidate<FULLFOV>(fd, QEntry<false>::make(dx.x, dy.x, d2.x, ja | gt),
-                                             live0, q2, q2n, wq, wqn, vball, a, counters);
+                    group_candidate<FULLFOV, TORUS>(
+                        fd, QEntry<false>::make(dx.x, dy.x, d2.x, ja | gt), live0, q2, q2n, wq,
+                        wqn, vball, a, counters);
                     if (second)
-                        group_candidate<FULLFOV>(fd,
-                                                 QEntry<false>::make(dx.y, dy.y, d2.y, jc | gt),
-                                                 live1, q2, q2n, wq, wqn, vball, a, counters);
+                        group_candidate<FULLFOV, TORUS>(
+                            fd, QEntry<false>::make(dx.y, dy.y, d2.y, jc | gt), live1, q2, q2n,
+                            wq, wqn, vball, a, counters);
                 } else {
                     const unsigned lm0 = __ballot_sync(ABM_FULL_MASK, live0);
                     const unsigned lm1 = __ballot_sync(ABM_FULL_MASK, live1);
@@ -1094,8 +1107,8 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
                     __syncwarp();
                     while (qn >= 32) {   // warp-uniform; at most two batches
                         qn -= 32;
-                        group_batch<true, FULLFOV>(fd, q + qn, 32, q2, q2n, wq, wqn, vball, a,
-                                                   counters);
+                        group_batch<true, FULLFOV, TORUS>(fd, q + qn, 32, q2, q2n, wq, wqn,
+                                                          vball, a, counters);
                     }
                 }
             }
@@ -1112,7 +1125,8 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
         todo &= ~members;
         scan(j0, n, members);
     }
-    if (qn > 0) group_batch<false, FULLFOV>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
+    if (qn > 0)
+        group_batch<false, FULLFOV, TORUS>(fd, q, qn, q2, q2n, wq, wqn, vball, a, counters);
     if (lane < wqn) {   // the last long or wrapping runs
         const int2 r = wq[lane];
         raster_projection(vball + (r.y >> kGroupTagShift) * words, a.g.rv, r.x,
@@ -1120,8 +1134,13 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
     }
     __syncwarp();
     // the last (< 32) deferred pairs
-    const unsigned nm =
-        q2n ? drain_deferred(fd, q2, q2n, vball, a.x, a.y, a.radius0, a.g) : 0u;
+    unsigned nm = 0u;
+    if (q2n) {
+        if constexpr (TORUS)
+            nm = drain_deferred_torus(fd, q2, q2n, vball, a.x, a.y, a.radius0, a.W, a.H, a.g);
+        else
+            nm = drain_deferred(fd, q2, q2n, vball, a.x, a.y, a.radius0, a.g);
+    }
     if (lane == 0 && q2n) {
         counters[0] += (unsigned)q2n;
         counters[1] += (unsigned)__popc(nm);
@@ -1611,8 +1630,7 @@ static int chunk_plan(int n, int c, int *off) {
     return r;
 }
 
-// group form (equal radii; one swarm, or walls in a batched sweep): chunks as in launch_l1,
-// counted in groups.
+// group form (equal radii): chunks as in launch_l1, counted in groups.
 static int launch_group(StepArgs a, int split, double arena_w, double arena_h,
                         cudaStream_t stream, int *chunks) {
     const int gsz = a.seg_begin ? kSegGroup : kGroup;
@@ -1650,14 +1668,25 @@ static int launch_group(StepArgs a, int split, double arena_w, double arena_h,
     const bool ff = a.g.full_fov != 0;
     cudaError_t e;
     if (a.seg_begin) {
-        // direct phase B when the whole arena lies within the cull radius (then every pair of
-        // agents inside it is live); any state is still handled exactly, only more slowly
-        const double ext2 = (double)arena_w * arena_w + (double)arena_h * arena_h;
+        // direct phase B when every offset between agents inside the arena (on the torus: every
+        // minimal image, at most half the extent) lies within the cull radius; any state is
+        // still handled exactly, only more slowly
+        const bool torus = a.ud.torus != 0;
+        double ext2 = (double)arena_w * arena_w + (double)arena_h * arena_h;
+        if (torus) ext2 *= 0.25;
         const bool direct = ext2 <= (double)a.radius0 * a.radius0 * a.g.cull;
-        if (ff && direct) e = launch_pdl(vpf_pairs_group_seg_kernel<true, true>, blocks, 32, smem, stream, a);
-        else if (ff) e = launch_pdl(vpf_pairs_group_seg_kernel<true, false>, blocks, 32, smem, stream, a);
-        else if (direct) e = launch_pdl(vpf_pairs_group_seg_kernel<false, true>, blocks, 32, smem, stream, a);
-        else e = launch_pdl(vpf_pairs_group_seg_kernel<false, false>, blocks, 32, smem, stream, a);
+        void (*kern)(StepArgs);
+        if (!torus)
+            kern = ff ? (direct ? vpf_pairs_group_seg_kernel<true, true, false>
+                                : vpf_pairs_group_seg_kernel<true, false, false>)
+                      : (direct ? vpf_pairs_group_seg_kernel<false, true, false>
+                                : vpf_pairs_group_seg_kernel<false, false, false>);
+        else
+            kern = ff ? (direct ? vpf_pairs_group_seg_kernel<true, true, true>
+                                : vpf_pairs_group_seg_kernel<true, false, true>)
+                      : (direct ? vpf_pairs_group_seg_kernel<false, true, true>
+                                : vpf_pairs_group_seg_kernel<false, false, true>);
+        e = launch_pdl(kern, blocks, 32, smem, stream, a);
     } else {
         const bool torus = a.ud.torus != 0;
         if (ff && !torus) e = launch_pdl(vpf_pairs_group_kernel<true, false>, blocks, 32, smem, stream, a);
@@ -2010,13 +2039,13 @@ static int step_launch(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
     const bool hetero = a.radius != nullptr;
     // auto: the l1 form while the positions fit comfortably in L1, tiled beyond; segmented
     // (batched) swarms always use the l1 form
-    // the group form: equal radii; on a torus one swarm whose width and height are floats
+    // the group form: equal radii; on a torus, width and height exact in float32
     const bool group_ok = !hetero && n < (1 << kGroupTagShift) &&
-                          (!torus || (!seg_begin && a.W.lo == 0.f && a.H.lo == 0.f));
+                          (!torus || (a.W.lo == 0.f && a.H.lo == 0.f));
     if (mode == 3 && !group_ok)
         return set_error(ABM_ERR_UNSUPPORTED,
-                         "%s: the group form needs equal radii (on a torus: one swarm, width and "
-                         "height exact in float32)", fn);
+                         "%s: the group form needs equal radii (on a torus: width and height "
+                         "exact in float32)", fn);
     // automatic: the group form for one swarm up to 16384 agents and for batched sweeps
     const bool use_group = group_ok && (mode == 3 || (mode == 0 && (seg_begin || n <= 16384)));
     const bool use_l1 = !use_group && (seg_begin || mode == 1 || (mode == 0 && n <= 16384));

@@ -175,8 +175,9 @@ int abm_vpf_flock_step(const abm_swarm_state *in, abm_swarm_state *out, int32_t 
  * agents are scheduled (put the largest instances first for load balance).  All instances share
  * p (Rv, arena, boundary, GAM, ALP1, BET1 ...).  Results per instance are bit-identical to
  * abm_vpf_flock_step on that instance alone.  Uses the group form of the pair kernel (groups
- * of 8 consecutive entries of the order) where it applies (walls, equal radii) and the L1 form
- * otherwise, unless abm_vpf_set_step_mode selects one.
+ * of 8 consecutive entries of the order) where it applies (equal radii; walls, or a torus whose
+ * width and height are exact in float32) and the L1 form otherwise, unless
+ * abm_vpf_set_step_mode selects one.
  */
 int abm_vpf_flock_batched(const abm_swarm_state *in, abm_swarm_state *out, int32_t n_total,
                           const int32_t *seg_begin_dev, const int32_t *seg_end_dev,
@@ -390,8 +391,8 @@ int abm_vpf_get_step_config(int32_t *warps_per_block, int32_t *tile);
  * block per focal agent, neighbours read through the read-only L1 path), 2 = tiled form
  * (warps_per_block focal agents share TMA-staged neighbour tiles), 3 = group form (one warp
  * per group of 4 consecutive focal agents, 8 in a batched sweep, each neighbour read once for
- * the group; equal radii, and on the infinite (torus) arena only for one swarm whose width
- * and height are exact in float32; otherwise the step returns ABM_ERR_UNSUPPORTED).
+ * the group; equal radii, and on the infinite (torus) arena a width and height exact in
+ * float32; otherwise the step returns ABM_ERR_UNSUPPORTED).
  * warps_per_agent in {1, 2, 4} splits one focal agent's neighbours over that many warps in the
  * L1 form; 0 keeps the current value.  All forms give bit-identical results. */
 int abm_vpf_set_step_mode(int32_t mode, int32_t warps_per_agent);

@@ -182,24 +182,27 @@ def test_polarisation_statistic_on_device():
     assert np.array_equal(b.polarisation(), pa)
 
 
+@pytest.mark.parametrize("boundary", ["walls", "infinite"])
 @pytest.mark.parametrize("width,fov", [(600.0, None), (600.0, (-1.5, 2.0)), (3000.0, None),
                                        (3000.0, (-1.5, 2.0))])
-def test_batched_group_kernel_forms_agree(width, fov):
-    """The batched group kernel's four forms -- phase B straight from the scan (an arena
-    inside the cull radius) or through the compaction queue (a larger arena), each with the
-    full field of view or a partial one -- against the L1 form on the same sweep: VPF, terms
-    and new state bit-identical."""
+def test_batched_group_kernel_forms_agree(width, fov, boundary):
+    """The batched group kernel's forms -- phase B straight from the scan (every offset inside
+    the cull radius) or through the compaction queue (a larger arena), each with the full
+    field of view or a partial one, between walls and on the torus (minimal images) -- against
+    the L1 form on the same sweep: VPF, terms and new state bit-identical."""
     import math
     from abm_gb300 import _lib
     from abm_gb300.batched import BatchedSweep, sweep_instances
     from abm_gb300.params import VFParams
     lib = _lib.load()
     kw = {} if fov is None else {"fov": fov}
-    vp = VFParams(alp1=0.08, bet1=0.08, width=width, height=width, rv=1200, **kw)
+    vp = VFParams(alp1=0.08, bet1=0.08, width=width, height=width, rv=1200, boundary=boundary,
+                  **kw)
     inst = sweep_instances(n_instances=9, n_min=10, n_max=260, alp_grid=(3, 3), seed=31,
                            width=width, height=width)
     cull = 10.0 / math.tan(2 * math.pi / 1200)   # h >= 1 only within this distance (R = 10)
-    assert (2 * width * width <= cull * cull) == (width < 1000.0)
+    ext2 = 2 * width * width if boundary == "walls" else width * width / 2
+    assert (ext2 <= cull * cull) == (width < 1000.0)
     outs = []
     try:
         for mode in (1, 3):
