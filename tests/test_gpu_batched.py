@@ -142,6 +142,47 @@ def test_batched_sweep_step_vs_oracle_every_instance():
     print(f"sweep: {b.n} agents, {tot_px} mismatched pixels, {tot_near} near-boundary pairs")
 
 
+@pytest.mark.parametrize("fov_ratio", [0.5, 1.0])
+def test_batched_torus_sweep_vs_oracle_every_instance(fov_ratio):
+    """A sweep shaped like the reference's torus experiments: 121 instances of N=10 on an
+    11 x 11 (ALP0, BET0) grid, a 900 x 900 torus, R = 5.5, field of view +-fov_ratio * pi with
+    Rv = 600 / fov_ratio (the metarunner's rescaling).  Rv = 1200 takes phase B straight from
+    the scan, Rv = 600 the compaction queue.  Every instance against the oracle's step from
+    the same state: VPF (excuse mask only), terms within 1e-5 relative, state within 2 ulps."""
+    import math
+    from abm_gb300.batched import BatchedSweep, sweep_instances
+    from abm_gb300.params import VFParams
+    rv = int(600 / fov_ratio)
+    vp = VFParams(alp1=0.08, bet1=0.08, width=900.0, height=900.0, rv=rv, radius=5.5,
+                  boundary="infinite", fov=(-fov_ratio * math.pi, fov_ratio * math.pi))
+    inst = sweep_instances(n_instances=121, n_min=10, n_max=10, alp_grid=(11, 11),
+                           alp_range=(0.0, 5.0), width=900.0, height=900.0, radius=5.5,
+                           seed=41)
+    rng = np.random.default_rng(41)
+    for d in inst:
+        d["v"] = rng.uniform(0, 1.5, len(d["x"])).astype(np.float32)
+    b = BatchedSweep(vp, inst)
+    b.step(want_vpf=True, want_terms=True)
+    bv, bt = b.vpf_numpy(), b.terms.cpu().numpy()
+    for k, d in enumerate(inst):
+        a0, a1 = int(b.offsets[k]), int(b.offsets[k + 1])
+        p = dict(vp.oracle_dict(), alp0=float(np.float32(d["alp0"])),
+                 bet0=float(np.float32(d["bet0"])))
+        st = {key: np.asarray(d[key], np.float32).astype(np.float64)
+              for key in ("x", "y", "theta", "v")}
+        ref = oracle.vf_step(st, p, want_excuse=True)
+        check_vpf(bv[a0:a1], ref["vpf"], ref["excuse"], ref["near"], k)
+        scale = np.maximum(np.abs(ref["terms"]), 1e-6)
+        err = np.abs(bt[a0:a1] - ref["terms"]) / scale
+        assert np.all(err <= 1e-5), (k, float(err.max()))
+        new = b.instance_state(k)
+        for key in ("x", "y", "theta", "v"):
+            r32 = ref[key].astype(np.float32)
+            ulp = np.spacing(np.abs(r32)).astype(np.float64)
+            diff = np.abs(new[key].astype(np.float64) - ref[key])
+            assert np.all(diff <= 2 * ulp + 1e-12), (k, key, float((diff / ulp).max()))
+
+
 def test_batched_graph_run_matches_eager_steps():
     from abm_gb300.batched import BatchedSweep
     from abm_gb300.params import VFParams
