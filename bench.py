@@ -396,7 +396,8 @@ def run_reference(args, rank, world):
 # ---------------------------------------------------------------------- batched sweep leg
 BATCHED = dict(workload="vf_batched_sweep", n_instances=512, n_per_instance="uniform int [10,500]",
                alp0_bet0="16 x 32 grid over [0.1, 3]", rv=1200, radius=10.0,
-               arena=[1000.0, 1000.0], boundary="walls", steps=2000, graph_chunk=100, seed=3)
+               arena=[1000.0, 1000.0], boundary="walls", steps=2000, graph_chunk=100, seed=3,
+               torus_steps=1000)
 
 
 def compact_table(tried):
@@ -500,6 +501,30 @@ def batched_leg(torch, lib, stream, steps=BATCHED["steps"], flush=None, rank=0, 
         e1.synchronize()
         t_graph = e0.elapsed_time(e1) * 1e-3 / (2 * reps)
     torch.cuda.current_stream().wait_stream(s)
+
+    # the same instances on a 1000 x 1000 torus (the boundary of the reference's current sweep
+    # experiments), automatic configuration, timed the same way
+    vt = VFParams(gam=0.1, v0=1.0, alp1=0.08, bet1=0.08, width=1000.0, height=1000.0,
+                  rv=BATCHED["rv"], radius=BATCHED["radius"], boundary="infinite")
+    bt = BatchedSweep(vt, inst)
+    bt.capture(chunk)
+    bt.run(chunk, chunk=chunk)                      # warm-up replay
+    torch.cuda.synchronize()
+    ev = []
+    done_t = 0
+    while done_t < BATCHED["torus_steps"]:
+        if flush is not None:
+            flush.fill_(float(done_t))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        bt.run(chunk, chunk=chunk)
+        e1.record()
+        ev.append((e0, e1))
+        done_t += chunk
+    torch.cuda.synchronize()
+    t_t = sum(a.elapsed_time(c) for a, c in ev) * 1e-3
+    (t_t,), torus_agent_steps = combine([t_t], bt.n * done_t, device=device)
+
     (t_b, t_eager, t_graph), agent_steps = combine([t_b, t_eager, t_graph], agent_steps,
                                                    device=device)
     n_tot = agent_steps // done
@@ -519,6 +544,9 @@ def batched_leg(torch, lib, stream, steps=BATCHED["steps"], flush=None, rank=0, 
                                       "per_rank": "each rank launches its own instances"
                                                   if world > 1 else None},
             "speedup_vs_per_instance_graph": t_graph / per_step,
+            "torus": {"boundary": "infinite", "config": "automatic", "steps": done_t,
+                      "value": torus_agent_steps / t_t, "unit": METRIC,
+                      "ms_per_step": t_t / done_t * 1e3, "gpu_launches": 2 * done_t},
             "autotune": {"best": tuned["best"], "table": compact_table(tuned["tried"])}}
 
 
