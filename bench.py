@@ -926,12 +926,13 @@ def profile_workload(which: str):
         for k in range(10):   # as in the timed region: the L2 flushed before every step
             flush.fill_(float(k))
             sw.step()
-    elif which == "batched":
+    elif which in ("batched", "batched_torus"):
         from abm_gb300.batched import BatchedSweep, sweep_instances
         from abm_gb300.params import VFParams
         B = BATCHED
         vp = VFParams(gam=0.1, v0=1.0, alp1=0.08, bet1=0.08, width=1000.0, height=1000.0,
-                      rv=B["rv"], radius=B["radius"])
+                      rv=B["rv"], radius=B["radius"],
+                      boundary="infinite" if which == "batched_torus" else "walls")
         b = BatchedSweep(vp, sweep_instances(n_instances=B["n_instances"], seed=B["seed"]))
         for _ in range(8):
             b.step()
@@ -974,7 +975,8 @@ def main():
                     help="repeat the timed K-step sequence until this much step time")
     ap.add_argument("--max-repeats", type=int, default=2000)
     ap.add_argument("--profile-workload",
-                    choices=["headline", "batched", "forage", "forage_collide", "edge"],
+                    choices=["headline", "batched", "batched_torus", "forage",
+                             "forage_collide", "edge"],
                     help="run a few eager steps of one leg's workload and exit (for ncu)")
     args = ap.parse_args()
     if args.profile_workload:
