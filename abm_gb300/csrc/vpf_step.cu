@@ -689,10 +689,11 @@ static __device__ __noinline__ unsigned drain_deferred_torus(const FocalDev *fd,
 // (e: the two-sum error).  It wraps iff it lies beyond +-L/2: L/2 is a float, d - L/2 is exact
 // wherever the sign of the sum is in doubt (Sterbenz), so fl(fl(d -+ L/2) + e) has the sign of
 // the exact comparison.  A wrapped offset is fl(fl(d -+ L) + e), exact up to the last rounding
-// for |d| <= 2L; `far` flags the offsets beyond that (positions more than 2L apart), which the
-// caller takes through the double-float offset.  An offset that does not wrap stays d, since
-// fl(d + e) = d.
-__device__ __forceinline__ float2 torus_image2(float2 d, float2 v, float f, float L, bool &far) {
+// for |d| <= 2L (the caller takes positions farther apart through the double-float offset).
+// An offset that does not wrap stays d, since fl(d + e) = d.  The wrap k in {-1, 0, 1} comes
+// from two compares as floats and d - kL from one fused multiply-add (kL is exact), which keeps
+// the selects off the ALU pipe.
+__device__ __forceinline__ float2 torus_image2(float2 d, float2 v, float f, float L) {
     const float2 nb = __fadd2_rn(v, make_float2(-d.x, -d.y));   // v - d
     const float2 t = __fadd2_rn(d, nb);                          // d - (d - v)
     const float2 e = __fadd2_rn(__fadd2_rn(v, make_float2(-t.x, -t.y)),
@@ -700,10 +701,32 @@ __device__ __forceinline__ float2 torus_image2(float2 d, float2 v, float f, floa
     const float h = 0.5f * L;
     const float2 up = __fadd2_rn(__fadd2_rn(d, make_float2(-h, -h)), e);
     const float2 dn = __fadd2_rn(__fadd2_rn(d, make_float2(h, h)), e);
-    const float wx = up.x > 0.f ? L : (dn.x < 0.f ? -L : 0.f);
-    const float wy = up.y > 0.f ? L : (dn.y < 0.f ? -L : 0.f);
-    far = fabsf(d.x) > 2.f * L || fabsf(d.y) > 2.f * L;
-    return __fadd2_rn(__fadd2_rn(d, make_float2(-wx, -wy)), e);
+    const float2 k = __fadd2_rn(make_float2(up.x > 0.f ? 1.f : 0.f, up.y > 0.f ? 1.f : 0.f),
+                                make_float2(dn.x < 0.f ? -1.f : 0.f, dn.y < 0.f ? -1.f : 0.f));
+    return __fadd2_rn(__ffma2_rn(make_float2(-L, -L), k, d), e);
+}
+
+// Whether a neighbour lies within 1.5 L (per axis) of every focal agent of a group: then every
+// offset of the group's pairs is at most 1.5 L < 2L, as torus_image2 needs (the window's
+// bounds are rounded inwards, so the test never admits a position outside it).  NaN positions
+// fail it.
+struct TorusWindow {
+    float xlo, xhi, ylo, yhi;
+    __device__ __forceinline__ bool holds(float x, float y) const {
+        return x >= xlo && x <= xhi && y >= ylo && y <= yhi;
+    }
+};
+
+__device__ __forceinline__ TorusWindow torus_window(const FocalDev *fd, int G, float W, float H) {
+    float x0 = fd[0].x, x1 = x0, y0 = fd[0].y, y1 = y0;
+    for (int g = 1; g < G; ++g) {
+        x0 = fminf(x0, fd[g].x);
+        x1 = fmaxf(x1, fd[g].x);
+        y0 = fminf(y0, fd[g].y);
+        y1 = fmaxf(y1, fd[g].y);
+    }
+    return {__fadd_ru(x1, -1.5f * W), __fadd_rd(x0, 1.5f * W), __fadd_ru(y1, -1.5f * H),
+            __fadd_rd(y0, 1.5f * H)};
 }
 
 // The offsets of the two neighbours (xv, yv) from focal agent f through the double-float
@@ -841,6 +864,8 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_kernel(const StepArgs 
     if (lane < G) fd[lane] = load_focal<false>(a, i0 + lane);   // the group's agents at once
     __syncwarp();
     const float cull_r2 = a.radius0 * a.radius0 * a.g.cull;
+    TorusWindow tw{};
+    if constexpr (TORUS) tw = torus_window(fd, G, a.W.hi, a.H.hi);
 
     int qn = 0, q2n = 0, wqn = 0;
     const unsigned lt = (1u << lane) - 1u;
@@ -864,16 +889,19 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_kernel(const StepArgs 
         const int jj = jb + 2 * lane;
         load2(jb + 64 + 2 * lane, xn2, yn2);   // prefetch the next round through L1
         const bool v0 = jj >= j0 && jj < n, v1 = jj + 1 >= j0 && jj + 1 < n;
+        bool far = false, anyfar = false;   // neighbours outside the group's torus window
+        if constexpr (TORUS) {
+            far = (v0 && !tw.holds(xv.x, yv.x)) || (v1 && !tw.holds(xv.y, yv.y));
+            anyfar = __any_sync(ABM_FULL_MASK, far);
+        }
         for (int g = 0; g < G; ++g) {   // warp-uniform
             const float fx = fd[g].x, fy = fd[g].y;
             float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
             float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
             if constexpr (TORUS) {
-                bool farx, fary;
-                dx = torus_image2(dx, xv, fx, a.W.hi, farx);
-                dy = torus_image2(dy, yv, fy, a.H.hi, fary);
-                const bool far = (v0 || v1) && (farx || fary);
-                if (__any_sync(ABM_FULL_MASK, far) && far) {
+                dx = torus_image2(dx, xv, fx, a.W.hi);
+                dy = torus_image2(dy, yv, fy, a.H.hi);
+                if (anyfar && far) {
                     const float4 o = torus_offsets_exact(fd, g, xv, yv, a.W, a.H);
                     dx = make_float2(o.x, o.y);
                     dy = make_float2(o.z, o.w);
@@ -1045,6 +1073,8 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
     }
     __syncwarp();
     const float cull_r2 = a.radius0 * a.radius0 * a.g.cull;
+    TorusWindow tw{};
+    if constexpr (TORUS) tw = torus_window(fd, G, a.W.hi, a.H.hi);
 
     int qn = 0, q2n = 0, wqn = 0;
     const unsigned lt = (1u << lane) - 1u;
@@ -1066,17 +1096,20 @@ __global__ void __launch_bounds__(32, 32) vpf_pairs_group_seg_kernel(const StepA
             load2(jb + 64, xn2, yn2);   // prefetch the next round through L1
             const bool v0 = ja < n, v1 = jc < n;
             const bool second = jb + 32 < n;   // warp-uniform
+            bool far = false, anyfar = false;   // neighbours outside the group's torus window
+            if constexpr (TORUS) {
+                far = (v0 && !tw.holds(xv.x, yv.x)) || (v1 && !tw.holds(xv.y, yv.y));
+                anyfar = __any_sync(ABM_FULL_MASK, far);
+            }
             for (int g = 0; g < G; ++g) {   // warp-uniform
                 if (!((members >> g) & 1u)) continue;
                 const float fx = fd[g].x, fy = fd[g].y;
                 float2 dx = __fadd2_rn(xv, make_float2(-fx, -fx));
                 float2 dy = __fadd2_rn(yv, make_float2(-fy, -fy));
                 if constexpr (TORUS) {
-                    bool farx, fary;
-                    dx = torus_image2(dx, xv, fx, a.W.hi, farx);
-                    dy = torus_image2(dy, yv, fy, a.H.hi, fary);
-                    const bool far = (v0 || v1) && (farx || fary);
-                    if (__any_sync(ABM_FULL_MASK, far) && far) {
+                    dx = torus_image2(dx, xv, fx, a.W.hi);
+                    dy = torus_image2(dy, yv, fy, a.H.hi);
+                    if (anyfar && far) {
                         const float4 o = torus_offsets_exact(fd, g, xv, yv, a.W, a.H);
                         dx = make_float2(o.x, o.y);
                         dy = make_float2(o.z, o.w);

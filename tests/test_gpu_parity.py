@@ -254,13 +254,14 @@ def test_group_form_torus_agrees(fov):
     """The group form on the torus (equal radii) against the L1 and tiled forms, bit for bit:
     a random swarm on a 1000 x 800 torus plus agents placed on the wrap seam (offsets of
     exactly W/2 and H/2, and offsets W/2 +- 1e-5 whose float32 difference rounds to W/2, on
-    either side), two agents whose images coincide, and agents more than 2W or 2H from others
-    (the double-float offset's path)."""
+    either side), two agents whose images coincide, and agents more than 2W or 2H from others,
+    one of them at x = 1e9 (the double-float offset's path)."""
     from abm_gb300.params import VFParams
     st = seeded_swarm(31, 1200, 1000.0, 800.0, pad=10.0, R=5.0)
     seam = [(-1e-5, 200.0), (500.0, 210.0), (1e-5, 220.0), (100.0, 230.0), (600.0, 240.0),
             (20.0, -1e-5), (30.0, 400.0), (40.0, 1e-5), (50.0, 50.0), (60.0, 450.0),
-            (0.0, 0.0), (1000.0, 0.0), (2600.0, 300.0), (300.0, 2000.0), (-2300.0, 500.0)]
+            (0.0, 0.0), (1000.0, 0.0), (2600.0, 300.0), (300.0, 2000.0), (-2300.0, 500.0),
+            (1.0e9, 100.0)]
     rng = np.random.default_rng(31)
     for k in ("x", "y"):
         extra = np.array([p[0 if k == "x" else 1] for p in seam], dtype=np.float32)
