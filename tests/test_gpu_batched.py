@@ -142,6 +142,39 @@ def test_batched_sweep_step_vs_oracle_every_instance():
     print(f"sweep: {b.n} agents, {tot_px} mismatched pixels, {tot_near} near-boundary pairs")
 
 
+def test_batched_torus_far_agents_forms_agree():
+    """Batched instances on a 600 x 600 torus with agents far outside it (x = 1500, -1300,
+    1e9; y = 1400): the group kernel takes their offsets through the double-float path and
+    equals the L1 form bit for bit (VPF, terms, new state), with and without direct phase B."""
+    from abm_gb300 import _lib
+    from abm_gb300.batched import BatchedSweep, sweep_instances
+    from abm_gb300.params import VFParams
+    lib = _lib.load()
+    inst = sweep_instances(n_instances=6, n_min=20, n_max=90, alp_grid=(2, 3), seed=51,
+                           width=600.0, height=600.0)
+    far = [(1500.0, 100.0), (-1300.0, 200.0), (1.0e9, 300.0), (100.0, 1400.0)]
+    for k, d in enumerate(inst[:4]):
+        d["x"][k % len(d["x"])] = np.float32(far[k][0])
+        d["y"][k % len(d["y"])] = np.float32(far[k][1])
+    outs = []
+    try:
+        for rv in (1200, 200):   # the arena within the cull radius (direct phase B) or not
+            vp = VFParams(alp1=0.08, bet1=0.08, width=600.0, height=600.0, rv=rv,
+                          boundary="infinite")
+            for mode in (1, 3):
+                _lib.check(lib.abm_vpf_set_step_mode(mode, 1))
+                b = BatchedSweep(vp, inst)
+                b.step(want_vpf=True, want_terms=True)
+                outs.append((rv, b.vpf_numpy(), b.terms.cpu().numpy(), b.state_numpy()))
+    finally:
+        lib.abm_vpf_set_step_mode(0, 1)
+    for a, b in ((outs[0], outs[1]), (outs[2], outs[3])):
+        assert np.array_equal(a[1], b[1]), a[0]
+        assert np.array_equal(a[2], b[2]), a[0]
+        for k in a[3]:
+            assert np.array_equal(a[3][k], b[3][k]), (a[0], k)
+
+
 @pytest.mark.parametrize("fov_ratio", [0.5, 1.0])
 def test_batched_torus_sweep_vs_oracle_every_instance(fov_ratio):
     """A sweep shaped like the reference's torus experiments: 121 instances of N=10 on an
